@@ -1,0 +1,158 @@
+"""CPU FP64 oracle for libcugpe's split-step evolution.
+
+TEST INFRASTRUCTURE ONLY.  Only ``tests/``, ``__graft_entry__.smoke()`` and
+the CPU-baseline leg of ``bench.py`` may import this package, and only as the
+checker or the timed CPU baseline.  The product (``libcugpe_gb300``) never
+imports it and has no CPU fallback.
+
+``gpe_oracle.c`` restates the reference algorithm (citations in its header);
+``np_oracle.py`` restates it again with numpy's FFT so the C restatement's own
+FFT can be cross-checked; ``build_ref.py`` builds the reference engine itself
+(on a machine with a GPU) for golden vectors and reference timings.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libgpe_oracle.so")
+
+INTER_GAMMA = {-1: 1.0, 0: 2.0, 1: 2.0}
+
+
+def build(force: bool = False) -> str:
+    src = os.path.join(HERE, "gpe_oracle.c")
+    if not force and os.path.isfile(LIB) and os.path.getmtime(LIB) > os.path.getmtime(src):
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    tmp = LIB + f".tmp{os.getpid()}"
+    # -ffp-contract=off keeps results identical on x86-64 and aarch64 hosts
+    cmd = ["gcc", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-std=gnu99",
+           src, "-o", tmp, "-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build()
+        L = ctypes.CDLL(path)
+        vp, d, i = ctypes.c_void_p, ctypes.c_double, ctypes.c_int
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.oracle_create.restype = vp
+        L.oracle_create.argtypes = [i, i, i, i, d, d, d, d, d]
+        L.oracle_destroy.argtypes = [vp]
+        L.oracle_set_threads.argtypes = [vp, i]
+        L.oracle_max_threads.restype = i
+        L.oracle_set_user_params.argtypes = [vp, i, dp]
+        L.oracle_set_user_params.restype = i
+        L.oracle_change_alpha_beta.argtypes = [vp, d, d]
+        L.oracle_set_time.argtypes = [vp, d]
+        L.oracle_set_qf.argtypes = [vp, d]
+        L.oracle_set_vextra.argtypes = [vp, dp, i, i]
+        L.oracle_set_psi.argtypes = [vp, d, dp]
+        L.oracle_get_psi.argtypes = [vp, dp, dp]
+        L.oracle_get_density.argtypes = [vp, dp, dp]
+        L.oracle_get_norm.argtypes = [vp]
+        L.oracle_get_norm.restype = d
+        L.oracle_normalize.argtypes = [vp]
+        L.oracle_evolve_qf.argtypes = [vp, i, dp]
+        L.oracle_evolve_qf.restype = i
+        L.oracle_energy.argtypes = [vp, dp, dp, dp, dp]
+        L.oracle_energy.restype = i
+        L.oracle_fft3d.argtypes = [i, i, i, dp, i, i]
+        _lib = L
+    return _lib
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Oracle:
+    """Mirror of the reference engine API (dev/gpe_engine.h:299-552) on the CPU."""
+
+    def __init__(self, shape, interactions, alpha, beta, dt, npart, gamma=None, threads=1):
+        self.shape = tuple(int(s) for s in shape)
+        self.gamma = INTER_GAMMA[interactions] if gamma is None else gamma
+        L = lib()
+        self._h = L.oracle_create(*self.shape, int(interactions), float(self.gamma),
+                                  float(alpha), float(beta), float(dt), float(npart))
+        if not self._h:
+            raise ValueError(f"unsupported lattice {shape}")
+        L.oracle_set_threads(self._h, int(threads))
+        self._vextra = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().oracle_destroy(h)
+            self._h = None
+
+    def set_threads(self, t):
+        lib().oracle_set_threads(self._h, int(t))
+
+    def set_user_params(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        return lib().oracle_set_user_params(self._h, len(p), _dp(p))
+
+    def change_alpha_beta(self, alpha, beta):
+        lib().oracle_change_alpha_beta(self._h, float(alpha), float(beta))
+
+    def set_time(self, t0):
+        lib().oracle_set_time(self._h, float(t0))
+
+    def set_quantum_friction_coeff(self, q):
+        lib().oracle_set_qf(self._h, float(q))
+
+    def set_vextra(self, fields, steps_per_slice):
+        self._vextra = np.ascontiguousarray(fields, dtype=np.float64)
+        lib().oracle_set_vextra(self._h, _dp(self._vextra), self._vextra.shape[0], int(steps_per_slice))
+
+    def set_psi(self, t, psi):
+        p = np.ascontiguousarray(psi, dtype=np.complex128).reshape(self.shape)
+        lib().oracle_set_psi(self._h, float(t), _dp(p.view(np.float64)))
+
+    def get_psi(self):
+        out = np.empty(self.shape, dtype=np.complex128)
+        t = ctypes.c_double()
+        lib().oracle_get_psi(self._h, ctypes.byref(t), _dp(out.view(np.float64)))
+        return t.value, out
+
+    def get_density(self):
+        out = np.empty(self.shape, dtype=np.float64)
+        t = ctypes.c_double()
+        lib().oracle_get_density(self._h, ctypes.byref(t), _dp(out))
+        return t.value, out
+
+    def get_norm(self):
+        return lib().oracle_get_norm(self._h)
+
+    def normalize_psi(self):
+        lib().oracle_normalize(self._h)
+
+    def evolve_qf(self, nt):
+        mu = ctypes.c_double(0.0)
+        lib().oracle_evolve_qf(self._h, int(nt), ctypes.byref(mu))
+        return mu.value
+
+    def energy(self):
+        t, a, b, c = (ctypes.c_double() for _ in range(4))
+        lib().oracle_energy(self._h, ctypes.byref(t), ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        return t.value, a.value, b.value, c.value
+
+
+def fft3d(a: np.ndarray, sign: int, threads: int = 1) -> np.ndarray:
+    out = np.ascontiguousarray(a, dtype=np.complex128).copy()
+    lib().oracle_fft3d(*out.shape, _dp(out.view(np.float64)), int(sign), int(threads))
+    return out

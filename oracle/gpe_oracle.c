@@ -1,0 +1,510 @@
+/*
+ * CPU FP64 restatement of libcugpe's split-step evolution (gpe_evolve_qf)
+ * and the observables around it.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle the CUDA engine is
+ * checked against and the timed CPU baseline; the product never links it.
+ *
+ * Every routine follows one reference routine, cited as file:line of
+ * KKobuszewski/libcugpe:
+ *   tables            dev/gpe_engine.cu:126-220 (gpe_reciprocal_lattice_init)
+ *   step coefficient  dev/gpe_engine.cu:177-181
+ *   density           dev/gpe_engine.cu:600-603
+ *   normalisation     dev/gpe_engine.cu:628-667
+ *   Vstep1/2/3, expT  dev/gpe_engine.cu:716-891
+ *   quantum friction  dev/gpe_engine.cu:893-933, 435-460
+ *   evolve loop       dev/gpe_engine.cu:1030-1109
+ *   energy            dev/gpe_engine.cu:1631-1705
+ *   functionals       dev/gpe_user_defined.h:118-135 (UFG), 196-243 (BEC side
+ *                     of the crossover), 305-322 (contact BEC)
+ *   harmonic trap     dev/gpe_user_defined.h:488-513
+ * The 3D FFT is cuFFT Z2Z in the reference (a third-party library absent from
+ * the reference tree): unnormalised, e^{-2 pi i jk/n} forward and e^{+...}
+ * inverse on a C-order [nx][ny][nz] array.  It is restated here as an
+ * iterative radix-2 transform per axis.  Sums use fixed-order pairwise
+ * summation over a fixed number of chunks (the reference's tree sum,
+ * dev/reductions.cu:64-130, differs only in order).
+ *
+ * Extension beyond the reference (used by the time-dependent control
+ * problem): an optional additive potential table, one real field per time
+ * slice, selected by it / steps_per_slice.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORC_MAX_USER_PARAMS 32
+#define ORC_QF_EPSILON 1.0e-12
+#define ORC_CHUNKS 256
+
+typedef struct { double x, y; } cd;
+
+static inline cd cmul(cd a, cd b) { cd c; c.x = a.x * b.x - a.y * b.y; c.y = a.x * b.y + a.y * b.x; return c; }
+static inline cd cscale(cd a, double s) { cd c; c.x = s * a.x; c.y = s * a.y; return c; }
+static inline cd cexp_(cd z) { double t = exp(z.x); cd r; r.x = t * cos(z.y); r.y = t * sin(z.y); return r; }
+
+typedef struct {
+    int nx, ny, nz;
+    size_t n;
+    int inter;            /* -1 contact BEC, 0 unitary Fermi gas, 1 BEC side of crossover */
+    double gamma;         /* 1 particles, 2 dimers */
+    double alpha, beta, dt, npart, t0, qfcoeff;
+    unsigned it;
+    double up[ORC_MAX_USER_PARAMS];
+    double *kx, *ky, *kz;
+    cd *ex, *ey, *ez;     /* ez includes 1/n */
+    cd c3;
+    cd *psi, *psi2, *wrkC, *wrk3C;
+    double *V, *Vqf, *rho;
+    cd *tw[3];            /* per-axis twiddles e^{-2 pi i k / n_axis}, k < n/2 */
+    int nthreads;
+    /* optional additive potential: nslices fields of n doubles */
+    const double *vextra;
+    int nslices, steps_per_slice;
+} gpe_oracle;
+
+/* ---------------------------------------------------------------- helpers */
+
+static double pairwise_sum(const double *a, size_t n) {
+    if (n <= 64) {
+        double s = 0.0;
+        for (size_t i = 0; i < n; i++) s += a[i];
+        return s;
+    }
+    size_t h = n / 2;
+    return pairwise_sum(a, h) + pairwise_sum(a + h, n - h);
+}
+
+/* deterministic sum: fixed chunking independent of the thread count */
+static double det_sum(const gpe_oracle *o, const double *a) {
+    double part[ORC_CHUNKS];
+    size_t n = o->n;
+    size_t chunk = (n + ORC_CHUNKS - 1) / ORC_CHUNKS;
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+    for (int c = 0; c < ORC_CHUNKS; c++) {
+        size_t b = (size_t)c * chunk, e = b + chunk;
+        if (b > n) b = n;
+        if (e > n) e = n;
+        part[c] = pairwise_sum(a + b, e - b);
+    }
+    return pairwise_sum(part, ORC_CHUNKS);
+}
+
+static void fill_k(double *k, int n) {
+    /* dev/gpe_engine.cu:147-154 */
+    int i, j;
+    for (i = 0; i <= n / 2 - 1; i++) k[i] = 2. * M_PI / n * (double)i;
+    j = -i;
+    for (i = n / 2; i < n; i++) { k[i] = 2. * M_PI / n * (double)j; j++; }
+}
+
+static void fill_tw(cd *tw, int n) {
+    for (int k = 0; k < n / 2; k++) {
+        long double a = -2.0L * 3.14159265358979323846264338327950288L * (long double)k / (long double)n;
+        tw[k].x = (double)cosl(a);
+        tw[k].y = (double)sinl(a);
+    }
+}
+
+/* in-place radix-2 FFT of a contiguous buffer; sign -1 forward, +1 inverse */
+static void fft1d(cd *a, int n, const cd *tw, int sign) {
+    for (int i = 1, j = 0; i < n; i++) {
+        int bit = n >> 1;
+        for (; j & bit; bit >>= 1) j ^= bit;
+        j ^= bit;
+        if (i < j) { cd t = a[i]; a[i] = a[j]; a[j] = t; }
+    }
+    for (int len = 2; len <= n; len <<= 1) {
+        int half = len >> 1, step = n / len;
+        for (int i = 0; i < n; i += len) {
+            for (int k = 0; k < half; k++) {
+                cd w = tw[k * step];
+                if (sign > 0) w.y = -w.y;
+                cd u = a[i + k], v = cmul(a[i + k + half], w);
+                a[i + k].x = u.x + v.x; a[i + k].y = u.y + v.y;
+                a[i + k + half].x = u.x - v.x; a[i + k + half].y = u.y - v.y;
+            }
+        }
+    }
+}
+
+/* unnormalised 3D transform of a C-order [nx][ny][nz] array */
+static void fft3d(const gpe_oracle *o, cd *a, int sign) {
+    const int nx = o->nx, ny = o->ny, nz = o->nz;
+    /* z: contiguous pencils */
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+    for (long p = 0; p < (long)nx * ny; p++) fft1d(a + (size_t)p * nz, nz, o->tw[2], sign);
+    /* y: stride nz */
+#pragma omp parallel num_threads(o->nthreads)
+    {
+        cd *buf = (cd *)malloc(sizeof(cd) * (size_t)ny);
+#pragma omp for schedule(static)
+        for (long p = 0; p < (long)nx * nz; p++) {
+            size_t ix = (size_t)p / nz, iz = (size_t)p % nz;
+            cd *base = a + ix * ny * nz + iz;
+            for (int j = 0; j < ny; j++) buf[j] = base[(size_t)j * nz];
+            fft1d(buf, ny, o->tw[1], sign);
+            for (int j = 0; j < ny; j++) base[(size_t)j * nz] = buf[j];
+        }
+        free(buf);
+    }
+    /* x: stride ny*nz */
+#pragma omp parallel num_threads(o->nthreads)
+    {
+        cd *buf = (cd *)malloc(sizeof(cd) * (size_t)nx);
+        const size_t s = (size_t)ny * nz;
+#pragma omp for schedule(static)
+        for (long p = 0; p < (long)s; p++) {
+            cd *base = a + p;
+            for (int j = 0; j < nx; j++) buf[j] = base[(size_t)j * s];
+            fft1d(buf, nx, o->tw[0], sign);
+            for (int j = 0; j < nx; j++) base[(size_t)j * s] = buf[j];
+        }
+        free(buf);
+    }
+}
+
+/* ----------------------------------------------------------- physics hooks */
+
+static inline double density(const gpe_oracle *o, cd p) { return o->gamma * (p.x * p.x + p.y * p.y); }
+
+static inline double vext(const gpe_oracle *o, size_t idx, int ix, int iy, int iz, unsigned it) {
+    /* dev/gpe_user_defined.h:488-513 */
+    const double wx = o->up[0], wy = o->up[1], wz = o->up[2];
+    const double _ix = (double)ix - 1.0 * (o->nx / 2);
+    const double _iy = (double)iy - 1.0 * (o->ny / 2);
+    const double _iz = (double)iz - 1.0 * (o->nz / 2);
+    double v = 0.5 * _ix * _ix * wx * wx + 0.5 * _iy * _iy * wy * wy + 0.5 * _iz * _iz * wz * wz;
+    if (o->vextra) {
+        int s = (int)(it / (unsigned)o->steps_per_slice);
+        if (s >= o->nslices) s = o->nslices - 1;
+        v += o->vextra[(size_t)s * o->n + idx];
+    }
+    return v;
+}
+
+#define ORC_XI 0.37
+#define ORC_CONTACT 0.901
+
+static inline double dEDFdn(const gpe_oracle *o, double rho) {
+    if (o->inter == 0) return 0.37 * pow(3.0 * M_PI * M_PI * rho, 2.0 / 3.0) / 2.0;
+    if (o->inter == -1) { const double a = o->up[3]; return 4 * M_PI * a * rho; }
+    if (o->inter == 1) {
+        const double a = o->up[3];
+        if (rho > 1e-15) {
+            const double kF = pow(3.0 * M_PI * M_PI * rho, 1.0 / 3.0);
+            const double eF = 0.5 * kF * kF;
+            const double x = (kF > 2.2250738585072014e-308) ? 1.0 / (a * kF) : 1.7976931348623157e308;
+            const double D = (ORC_XI + x * (1.0 + ORC_CONTACT) + 3.0 * M_PI * ORC_XI * x * x);
+            return ORC_XI * eF * (ORC_XI + 0.8 * x) / D
+                 + 0.2 * ORC_XI * eF * (ORC_XI + x) * x * ((1.0 + ORC_CONTACT) + 6.0 * M_PI * ORC_XI * x) / (D * D)
+                 - 1.0 / (2.0 * a * a);
+        }
+        return -1.0 / (2.0 * a * a);
+    }
+    return 0.0;
+}
+
+static inline double EDF(const gpe_oracle *o, double rho) {
+    if (o->inter == 0) return 0.37 * 0.6 * rho * pow(3.0 * M_PI * M_PI * rho, 2.0 / 3.0) / 2.;
+    if (o->inter == -1) { const double a = o->up[3]; return 2 * M_PI * a * rho * rho; }
+    if (o->inter == 1) {
+        const double a = o->up[3];
+        const double kF = pow(3.0 * M_PI * M_PI * rho, 1.0 / 3.0);
+        const double eF = 0.5 * kF * kF;
+        const double x = (kF > 2.2250738585072014e-308) ? 1.0 / (a * kF) : 1.7976931348623157e308;
+        return 0.6 * eF * rho * ORC_XI * (ORC_XI + x) / (ORC_XI + x * (1.0 + ORC_CONTACT) + 3.0 * M_PI * ORC_XI * x * x)
+             - rho / (2.0 * a * a);
+    }
+    return 0.0;
+}
+
+/* -------------------------------------------------------------- lifecycle */
+
+static void tables(gpe_oracle *o) {
+    /* dev/gpe_engine.cu:177-216: c3 = Gamma*0.5*dt / (-beta + i alpha) */
+    const double a = o->gamma * 0.5 * o->dt;
+    const double br = -1.0 * o->beta, bi = o->alpha;
+    const double den = br * br + bi * bi;
+    o->c3.x = a * br / den;
+    o->c3.y = -a * bi / den;
+    const double g2 = o->gamma * o->gamma;
+    for (int i = 0; i < o->nx; i++) {
+        cd z = o->c3; z = cscale(z, o->kx[i]); z = cscale(z, o->kx[i]); z.x /= g2; z.y /= g2;
+        o->ex[i] = cexp_(z);
+    }
+    for (int i = 0; i < o->ny; i++) {
+        cd z = o->c3; z = cscale(z, o->ky[i]); z = cscale(z, o->ky[i]); z.x /= g2; z.y /= g2;
+        o->ey[i] = cexp_(z);
+    }
+    for (int i = 0; i < o->nz; i++) {
+        cd z = o->c3; z = cscale(z, o->kz[i]); z = cscale(z, o->kz[i]); z.x /= g2; z.y /= g2;
+        z = cexp_(z);
+        z.x /= (double)o->n; z.y /= (double)o->n;
+        o->ez[i] = z;
+    }
+}
+
+void *oracle_create(int nx, int ny, int nz, int inter, double gamma,
+                    double alpha, double beta, double dt, double npart) {
+    if (nx < 2 || ny < 2 || nz < 2) return NULL;
+    if ((nx & (nx - 1)) || (ny & (ny - 1)) || (nz & (nz - 1))) return NULL;
+    gpe_oracle *o = (gpe_oracle *)calloc(1, sizeof(gpe_oracle));
+    o->nx = nx; o->ny = ny; o->nz = nz;
+    o->n = (size_t)nx * ny * nz;
+    o->inter = inter; o->gamma = gamma;
+    o->alpha = alpha; o->beta = beta; o->dt = dt; o->npart = npart;
+    o->nthreads = 1;
+    o->kx = malloc(sizeof(double) * nx); o->ky = malloc(sizeof(double) * ny); o->kz = malloc(sizeof(double) * nz);
+    fill_k(o->kx, nx); fill_k(o->ky, ny); fill_k(o->kz, nz);
+    o->ex = malloc(sizeof(cd) * nx); o->ey = malloc(sizeof(cd) * ny); o->ez = malloc(sizeof(cd) * nz);
+    int ns[3] = {nx, ny, nz};
+    for (int a = 0; a < 3; a++) { o->tw[a] = malloc(sizeof(cd) * (ns[a] / 2 + 1)); fill_tw(o->tw[a], ns[a]); }
+    tables(o);
+    o->psi = calloc(o->n, sizeof(cd)); o->psi2 = calloc(o->n, sizeof(cd));
+    o->wrkC = calloc(o->n, sizeof(cd)); o->wrk3C = calloc(o->n, sizeof(cd));
+    o->V = calloc(o->n, sizeof(double)); o->Vqf = calloc(o->n, sizeof(double)); o->rho = calloc(o->n, sizeof(double));
+    return o;
+}
+
+void oracle_destroy(void *h) {
+    gpe_oracle *o = (gpe_oracle *)h;
+    if (!o) return;
+    free(o->kx); free(o->ky); free(o->kz); free(o->ex); free(o->ey); free(o->ez);
+    for (int a = 0; a < 3; a++) free(o->tw[a]);
+    free(o->psi); free(o->psi2); free(o->wrkC); free(o->wrk3C); free(o->V); free(o->Vqf); free(o->rho);
+    free(o);
+}
+
+void oracle_set_threads(void *h, int t) { ((gpe_oracle *)h)->nthreads = t > 0 ? t : 1; }
+
+int oracle_max_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+int oracle_set_user_params(void *h, int size, const double *p) {
+    gpe_oracle *o = (gpe_oracle *)h;
+    if (size > ORC_MAX_USER_PARAMS || size < 0) return -9;
+    memset(o->up, 0, sizeof o->up);
+    memcpy(o->up, p, sizeof(double) * (size_t)size);
+    return 0;
+}
+
+void oracle_change_alpha_beta(void *h, double alpha, double beta) {
+    gpe_oracle *o = (gpe_oracle *)h;
+    o->alpha = alpha; o->beta = beta;
+    tables(o);
+}
+
+void oracle_set_time(void *h, double t0) { gpe_oracle *o = (gpe_oracle *)h; o->t0 = t0; o->it = 0; }
+
+void oracle_set_qf(void *h, double q) {
+    /* dev/gpe_engine.cu:435-460 */
+    gpe_oracle *o = (gpe_oracle *)h;
+    o->qfcoeff = (q != 0.0) ? q / (o->gamma * (double)o->n) : 0.0;
+}
+
+void oracle_set_vextra(void *h, const double *v, int nslices, int steps_per_slice) {
+    gpe_oracle *o = (gpe_oracle *)h;
+    o->vextra = v; o->nslices = nslices; o->steps_per_slice = steps_per_slice > 0 ? steps_per_slice : 1;
+}
+
+void oracle_set_psi(void *h, double t, const double *psi) {
+    gpe_oracle *o = (gpe_oracle *)h;
+    o->t0 = t; o->it = 0;
+    memcpy(o->psi, psi, sizeof(cd) * o->n);
+}
+
+void oracle_get_psi(void *h, double *t, double *psi) {
+    gpe_oracle *o = (gpe_oracle *)h;
+    memcpy(psi, o->psi, sizeof(cd) * o->n);
+    if (t) *t = o->t0 + o->dt * o->it;
+}
+
+/* ------------------------------------------------------------- operations */
+
+static double norm_of(gpe_oracle *o, const cd *p) {
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+    for (long i = 0; i < (long)o->n; i++) o->rho[i] = density(o, p[i]);
+    return det_sum(o, o->rho);
+}
+
+static double normalize(gpe_oracle *o, cd *p) {
+    /* dev/gpe_engine.cu:628-646 */
+    const double sum = norm_of(o, p);
+    const double s = sqrt(o->npart / sum);
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+    for (long i = 0; i < (long)o->n; i++) p[i] = cscale(p[i], s);
+    return sum;
+}
+
+void oracle_get_density(void *h, double *t, double *out) {
+    gpe_oracle *o = (gpe_oracle *)h;
+    for (size_t i = 0; i < o->n; i++) out[i] = density(o, o->psi[i]);
+    if (t) *t = o->t0 + o->dt * o->it;
+}
+
+double oracle_get_norm(void *h) { gpe_oracle *o = (gpe_oracle *)h; return norm_of(o, o->psi); }
+
+void oracle_normalize(void *h) { gpe_oracle *o = (gpe_oracle *)h; normalize(o, o->psi); }
+
+#define DECODE(i)                                   \
+    const int ix = (int)((i) / ((size_t)ny * nz));  \
+    const int iy = (int)(((i) / nz) % ny);          \
+    const int iz = (int)((i) % nz);
+
+static void mult_expT(gpe_oracle *o, cd *p) {
+    /* dev/gpe_engine.cu:876-891 */
+    const int ny = o->ny, nz = o->nz;
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+    for (long i = 0; i < (long)o->n; i++) {
+        DECODE((size_t)i);
+        cd w = p[i];
+        w = cmul(w, o->ex[ix]);
+        w = cmul(w, o->ey[iy]);
+        w = cmul(w, o->ez[iz]);
+        p[i] = w;
+    }
+}
+
+static void qf_potential(gpe_oracle *o, const cd *psi) {
+    /* dev/gpe_engine.cu:893-933 */
+    const int ny = o->ny, nz = o->nz;
+    memcpy(o->wrk3C, psi, sizeof(cd) * o->n);
+    fft3d(o, o->wrk3C, -1);
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+    for (long i = 0; i < (long)o->n; i++) {
+        DECODE((size_t)i);
+        o->wrk3C[i] = cscale(o->wrk3C[i], o->qfcoeff * (o->kx[ix] * o->kx[ix] + o->ky[iy] * o->ky[iy] + o->kz[iz] * o->kz[iz]));
+    }
+    fft3d(o, o->wrk3C, +1);
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+    for (long i = 0; i < (long)o->n; i++) {
+        cd a = psi[i]; a.y = -a.y;
+        const cd b = o->wrk3C[i];
+        const double lrho = density(o, psi[i]);
+        o->Vqf[i] = (a.x * b.y + a.y * b.x) / (lrho + ORC_QF_EPSILON);
+    }
+}
+
+int oracle_evolve_qf(void *h, int nt, double *mu) {
+    gpe_oracle *o = (gpe_oracle *)h;
+    const int ny = o->ny, nz = o->nz;
+    const long n = (long)o->n;
+    const int qf = o->qfcoeff != 0.0;
+    for (int step = 0; step < nt; step++) {
+        const unsigned it = o->it;
+        /* Vstep1 / Vstep1_qf: dev/gpe_engine.cu:719-768, 1038-1047 */
+        if (qf) qf_potential(o, o->psi);
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+        for (long i = 0; i < n; i++) {
+            DECODE((size_t)i);
+            const cd lpsi = o->psi[i];
+            const double lrho = density(o, lpsi);
+            double lv = vext(o, (size_t)i, ix, iy, iz, it) + dEDFdn(o, lrho);
+            if (qf) lv += o->Vqf[i];
+            o->V[i] = lv;
+            o->psi2[i] = cmul(lpsi, cexp_(cscale(o->c3, lv)));
+        }
+        /* kinetic: dev/gpe_engine.cu:1050-1054 */
+        fft3d(o, o->psi2, -1);
+        mult_expT(o, o->psi2);
+        fft3d(o, o->psi2, +1);
+        if (o->beta == 0.0 && !qf) {
+            /* Vstep2: dev/gpe_engine.cu:770-797 */
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+            for (long i = 0; i < n; i++) {
+                DECODE((size_t)i);
+                double lv = o->V[i];
+                cd lpsi = cmul(o->psi2[i], cexp_(cscale(o->c3, lv)));
+                const double lrho = density(o, lpsi);
+                lv = 0.5 * (lv + vext(o, (size_t)i, ix, iy, iz, it + 1) + dEDFdn(o, lrho));
+                const cd e = cexp_(cscale(o->c3, lv));
+                o->wrkC[i] = e;
+                o->psi[i] = cmul(o->psi[i], e);
+            }
+        } else {
+            /* part1: dev/gpe_engine.cu:799-811 */
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+            for (long i = 0; i < n; i++) o->psi2[i] = cmul(o->psi2[i], cexp_(cscale(o->c3, o->V[i])));
+            if (o->beta != 0.0) normalize(o, o->psi2);
+            if (qf) qf_potential(o, o->psi);
+            /* part2 / part2_qf: dev/gpe_engine.cu:813-864 */
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+            for (long i = 0; i < n; i++) {
+                DECODE((size_t)i);
+                const double lrho = density(o, o->psi2[i]);
+                double lv = o->V[i] + vext(o, (size_t)i, ix, iy, iz, it + 1) + dEDFdn(o, lrho);
+                if (qf) lv += o->Vqf[i];
+                lv = 0.5 * lv;
+                const cd e = cexp_(cscale(o->c3, lv));
+                o->wrkC[i] = e;
+                o->psi[i] = cmul(o->psi[i], e);
+            }
+        }
+        fft3d(o, o->psi, -1);
+        mult_expT(o, o->psi);
+        fft3d(o, o->psi, +1);
+        /* Vstep3: dev/gpe_engine.cu:866-874 */
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+        for (long i = 0; i < n; i++) o->psi[i] = cmul(o->psi[i], o->wrkC[i]);
+        if (o->beta != 0.0) {
+            const double norm = normalize(o, o->psi);
+            if (mu) *mu = -.5 * log(norm / o->npart) / o->dt;
+        }
+        o->it = o->it + 1;
+    }
+    return 0;
+}
+
+int oracle_energy(void *h, double *t, double *ekin, double *eint, double *eext) {
+    /* dev/gpe_engine.cu:1669-1705 */
+    gpe_oracle *o = (gpe_oracle *)h;
+    const int ny = o->ny, nz = o->nz;
+    const long n = (long)o->n;
+    *t = o->t0 + o->dt * o->it;
+    if (o->beta == 0.0) normalize(o, o->psi);
+    double *w1 = (double *)malloc(sizeof(double) * n), *w2 = (double *)malloc(sizeof(double) * n);
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+    for (long i = 0; i < n; i++) {
+        DECODE((size_t)i);
+        const double lrho = density(o, o->psi[i]);
+        w1[i] = lrho * vext(o, (size_t)i, ix, iy, iz, o->it);
+        w2[i] = EDF(o, lrho);
+    }
+    *eext = det_sum(o, w1);
+    *eint = det_sum(o, w2);
+    memcpy(o->psi2, o->psi, sizeof(cd) * o->n);
+    fft3d(o, o->psi2, -1);
+    const double den = 2.0 * o->gamma * (double)o->n;
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+    for (long i = 0; i < n; i++) {
+        DECODE((size_t)i);
+        o->psi2[i] = cscale(o->psi2[i], (o->kx[ix] * o->kx[ix] + o->ky[iy] * o->ky[iy] + o->kz[iz] * o->kz[iz]) / den);
+    }
+    fft3d(o, o->psi2, +1);
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+    for (long i = 0; i < n; i++) w1[i] = o->psi[i].x * o->psi2[i].x + o->psi[i].y * o->psi2[i].y;
+    *ekin = det_sum(o, w1);
+    free(w1); free(w2);
+    return 0;
+}
+
+/* raw 3D transform, exposed so the tests can pin the restated FFT against numpy */
+void oracle_fft3d(int nx, int ny, int nz, double *a, int sign, int nthreads) {
+    gpe_oracle o;
+    memset(&o, 0, sizeof o);
+    o.nx = nx; o.ny = ny; o.nz = nz; o.n = (size_t)nx * ny * nz; o.nthreads = nthreads > 0 ? nthreads : 1;
+    int ns[3] = {nx, ny, nz};
+    for (int k = 0; k < 3; k++) { o.tw[k] = malloc(sizeof(cd) * (ns[k] / 2 + 1)); fill_tw(o.tw[k], ns[k]); }
+    fft3d(&o, (cd *)a, sign);
+    for (int k = 0; k < 3; k++) free(o.tw[k]);
+}
