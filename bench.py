@@ -1,0 +1,352 @@
+"""Benchmark of the split-step evolution (libcugpe's gpe_evolve_qf path) on GB300.
+
+Workload (one condensate per GPU): 128^3 unitary Fermi gas (dimers), real-time
+evolution with quantum friction 0.1, dx = 0.2, trap omega = (1, 1, 1.5),
+dt = 5e-3 (lattice dt' = 0.125), npart = 1000, starting from an imaginary-time
+relaxed Thomas-Fermi state with the vortex phase atan2(y, x) imprinted.
+Synthetic, seeded (numpy PCG64, seed 0).
+
+A timed step is one gpe_evolve_qf(BLOCK) call (BLOCK GPE time steps, default
+100) of the FP32-mixed engine; L2 is flushed (256 MiB write) before every timed
+step.  `value` is GPE time steps per second with the state resident in HBM;
+`e2e` is the same through the C ABI with host buffers: gpe_set_psi (host
+complex128 -> device), gpe_evolve_qf(BLOCK), gpe_get_psi (device -> host).
+The plain FP64 drop-in, the FP32 energy error against it, the reference
+libcugpe engine on the same GPU (when its edited sources are present) and the
+CPU FP64 oracle are reported beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+B_ALG = {  # algorithmic bytes per grid point per step (8 S + S + 4 s_r, + 4 S with quantum friction)
+    ("fp32", True): 120, ("fp32", False): 88, ("fp64", True): 240, ("fp64", False): 176,
+}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=10)
+            self.fh.close()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax = float(f[1])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, x):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def workload(n):
+    from libcugpe_gb300 import configs
+    return configs.ufg_vortex_rte_qf(n=n)
+
+
+def relaxed_state(w, ite_steps):
+    """Imaginary-time relaxation of the Thomas-Fermi start, then the vortex phase."""
+    import libcugpe_gb300 as g
+    from libcugpe_gb300 import configs
+    amp = np.abs(w.psi0)
+    e = g.Engine(w.shape, w.interactions, 0.0, 1.0, w.dt, w.npart, precision=g.FP32)
+    e.set_user_params(w.params)
+    e.set_psi(0.0, amp)
+    e.evolve_qf(ite_steps)
+    _, psi = e.get_psi()
+    e.close()
+    X, Y, _ = configs.grid(w.shape)
+    return np.abs(psi) * np.exp(1j * np.arctan2(Y + 0.5, X + 0.5))
+
+
+def make_engine(w, psi, precision):
+    import libcugpe_gb300 as g
+    e = g.Engine(w.shape, w.interactions, w.alpha, w.beta, w.dt, w.npart, precision=precision)
+    e.set_user_params(w.params)
+    e.set_quantum_friction_coeff(w.qf)
+    e.set_psi(0.0, psi)
+    return e
+
+
+def time_blocks(e, block, steps, warmup, flush, torch):
+    """Device time of `steps` evolve_qf(block) calls, L2 flushed before each."""
+    stream = torch.cuda.ExternalStream(e.stream_handle())
+    for _ in range(warmup):
+        e.evolve_qf(block)
+    torch.cuda.synchronize()
+    total = 0.0
+    l0 = e.kernel_launches()
+    for _ in range(steps):
+        flush.add_(1.0)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        e.evolve_qf(block)
+        b.record(stream)
+        b.synchronize()
+        total += a.elapsed_time(b) / 1e3
+    return total, e.kernel_launches() - l0
+
+
+def time_e2e(e, block, steps, host_psi, flush, torch):
+    """The same through the C ABI with host buffers (H2D + evolve + D2H per step)."""
+    stream = torch.cuda.ExternalStream(e.stream_handle())
+    total = 0.0
+    for _ in range(steps):
+        flush.add_(1.0)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        e.set_psi(0.0, host_psi)
+        e.evolve_qf(block)
+        e.get_psi(out=host_psi)
+        b.record(stream)
+        b.synchronize()
+        total += a.elapsed_time(b) / 1e3
+    return total
+
+
+def cpu_baseline(w, psi, seconds=15.0):
+    """The CPU FP64 oracle on all host threads, a bounded number of steps."""
+    import oracle
+    threads = len(os.sched_getaffinity(0))
+    o = oracle.Oracle(w.shape, w.interactions, w.alpha, w.beta, w.dt, w.npart, threads=threads)
+    o.set_user_params(w.params)
+    o.set_quantum_friction_coeff(w.qf)
+    o.set_psi(0.0, psi)
+    o.evolve_qf(1)
+    steps, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds or steps < 2:
+        o.evolve_qf(1)
+        steps += 1
+    dt = time.perf_counter() - t0
+    return {"value": steps / dt, "unit": "steps/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} steps of the {w.shape[0]}^3 workload in {dt:.1f} s (oracle/gpe_oracle.c, FP64, OpenMP)"}
+
+
+def reference_gpu(w, psi, steps=20):
+    """The reference libcugpe engine (cuFFT Z2Z, FP64) built for this GPU, if its sources are here."""
+    try:
+        from oracle import build_ref, ref_run
+        if not ref_run.available():
+            return None
+        nx, ny, nz = w.shape
+        build_ref.build_one(nx, ny, nz, w.interactions)
+        out = ref_run.run(w.shape, w.interactions, w.alpha, w.beta, w.dt, w.npart, w.params, psi,
+                          ["S5", f"B{steps}", f"B{steps}"], qf=w.qf)
+        ms = min(out["time_ms"])
+        return {"value": steps / (ms / 1e3), "unit": "steps/s", "dtype": "f64",
+                "what": "reference libcugpe dev/ engine (cuFFT Z2Z) built for sm_103a, CUDA events around gpe_evolve_qf"}
+    except Exception as ex:  # reported, never fatal
+        return {"unavailable": str(ex)[:200]}
+
+
+def run_reference_arm(args, ws, rank):
+    """--impl reference: the reference path timed on the host cores (the oracle port)."""
+    if rank != 0:
+        return
+    w = workload(args.n)
+    import oracle
+    threads = len(os.sched_getaffinity(0))
+    o = oracle.Oracle(w.shape, w.interactions, w.alpha, w.beta, w.dt, w.npart, threads=threads)
+    o.set_user_params(w.params)
+    o.set_quantum_friction_coeff(w.qf)
+    o.set_psi(0.0, w.psi0)
+    per = max(1, args.cpu_steps)
+    for _ in range(args.warmup):
+        o.evolve_qf(1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.evolve_qf(per)
+    dt = time.perf_counter() - t0
+    v = args.steps * per / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "config": config_obj(w, args),
+            "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} x {per} steps of the {w.shape[0]}^3 workload "
+                                       "(oracle/gpe_oracle.c FP64 restatement; the reference has no CPU path)"},
+            "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+METRIC = "128^3 GPE steps/s (FP32-mixed split-step, UFG + quantum friction RTE)"
+
+
+def config_obj(w, args):
+    return {"workload": f"{w.shape[0]}^3 unitary Fermi gas RTE + quantum friction 0.1, dx=0.2, dt=5e-3, "
+                        f"omega=(1,1,1.5), npart=1000, vortex start",
+            "lattice": list(w.shape), "gpe_steps_per_timed_step": args.block, "precision": "fp32-mixed",
+            "l2": "flushed (256 MiB write) before every timed step; the 128^3 FP32 working set stays in L2 within a step",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--block", type=int, default=100)
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--no-extras", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference_arm(args, ws, rank)
+        return
+
+    import torch
+    import libcugpe_gb300 as g
+    torch.cuda.set_device(local)
+    w = workload(args.n)
+    psi = relaxed_state(w, 200)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+
+    e32 = make_engine(w, psi, g.FP32)
+    barrier(ws)
+    with Clocks(local) as clk:
+        t32, launches = time_blocks(e32, args.block, args.steps, args.warmup, flush, torch)
+    t32 = max_over_ranks(ws, t32)
+    value = ws * args.steps * args.block / t32
+
+    host = torch.empty(w.shape + (2,), dtype=torch.float64, pin_memory=True).numpy().view(np.complex128)[..., 0]
+    host[...] = psi
+    te2e = time_e2e(e32, args.block, max(2, args.steps // 2), host, flush, torch)
+    te2e = max_over_ranks(ws, te2e)
+    e2e_value = ws * max(2, args.steps // 2) * args.block / te2e
+
+    extras = {}
+    if not args.no_extras and rank == 0:
+        # plain FP64 drop-in on the same workload
+        e64 = make_engine(w, psi, g.FP64)
+        b64 = max(5, args.block // 10)
+        t64, _ = time_blocks(e64, b64, 3, 1, flush, torch)
+        extras["fp64_plain"] = {"value": 3 * b64 / t64, "unit": "steps/s", "dtype": "f64"}
+        # FP32 energy and density error against the FP64 form after the same steps
+        a = make_engine(w, psi, g.FP32)
+        b = make_engine(w, psi, g.FP64)
+        nchk = 200
+        a.evolve_qf(nchk)
+        b.evolve_qf(nchk)
+        ea, eb = a.energy(), b.energy()
+        Ea, Eb = sum(ea[1:]), sum(eb[1:])
+        _, da = a.get_density()
+        _, db = b.get_density()
+        extras["fp32_vs_fp64"] = {"steps": nchk, "dE_over_E": abs(Ea - Eb) / abs(Eb),
+                                  "density_rel_l2": float(np.linalg.norm(da - db) / np.linalg.norm(db))}
+        a.close(); b.close(); e64.close()
+        ref = reference_gpu(w, psi)
+        if ref:
+            extras["reference_gpu"] = ref
+        extras["cpu_baseline"] = cpu_baseline(w, psi, seconds=args.cpu_seconds if hasattr(args, "cpu_seconds") else 15.0)
+
+    if rank == 0:
+        n = int(np.prod(w.shape))
+        peak, kind = peaks()
+        achieved = B_ALG[("fp32", True)] * n * (value / ws) / 1e9
+        clk_s = clk.summary()
+        line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * t32 / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+                "config": config_obj(w, args),
+                "points_steps_per_s": value * n,
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": None,
+                             "basis": f"B_alg {B_ALG[('fp32', True)]} B/pt/step x {n} pts / step time; peak {kind}"},
+                "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": 16 * n,
+                        "d2h_bytes_per_step": 16 * n},
+                "gpu_launches": launches, "clocks": clk_s}
+        line.update(extras)
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

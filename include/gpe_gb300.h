@@ -1,0 +1,96 @@
+/*
+ * C ABI of the GB300 split-step GPE engine (libgpe_gb300.so).
+ *
+ * Plain pointers and sizes only.  Each entry point is a handle-based form of
+ * one reference engine call (KKobuszewski/libcugpe, dev/gpe_engine.h); the
+ * reference's own C++-linkage, single-global-engine signatures are declared
+ * in gpe_engine.h and implemented on top of these.
+ *
+ * Wavefunctions cross the boundary as interleaved complex128 (the reference's
+ * cuDoubleComplex), C order [nx][ny][nz] with z fastest, in host memory
+ * (pinned or pageable), exactly as gpe_set_psi / gpe_get_psi take them.
+ *
+ * Return codes: 0 on success; a positive value is the cudaError_t of the
+ * failing CUDA call (as the reference's cuErrCheck, dev/gpe_engine.h:201-209);
+ * negative values are the GPE_ERR_* codes below (-9 is the reference's
+ * "too many user parameters", dev/gpe_engine.cu:428).
+ */
+#ifndef GPE_GB300_H
+#define GPE_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GPE_ERR_TOO_MANY_PARAMS (-9)   /* dev/gpe_engine.cu:428 */
+#define GPE_ERR_LATTICE (-10)          /* side not a power of two in [8, 512] */
+#define GPE_ERR_NO_ENGINE (-11)        /* null handle / engine not created */
+#define GPE_ERR_ARGUMENT (-12)         /* null pointer or bad value */
+#define GPE_ERR_FUNCTIONAL (-13)       /* unknown interactions code */
+#define GPE_ERR_NOT_IMPLEMENTED (-98)  /* reference entry point outside this engine */
+
+#define GPE_PRECISION_FP64 0 /* plain FP64 drop-in */
+#define GPE_PRECISION_FP32 1 /* FP32 field/FFT/phases, FP64 tables and reductions */
+
+typedef struct gpe_gb_engine gpe_gb_engine;
+
+/* gpe_create_engine (dev/gpe_engine.cu:286), with the lattice and functional
+ * that the reference fixes at compile time (NX/NY/NZ, INTERACTIONS) given at
+ * run time.  interactions: -1 contact BEC, 0 unitary Fermi gas (dimers),
+ * 1 BEC side of the crossover (dimers). */
+int gpe_gb_create(gpe_gb_engine** out, int nx, int ny, int nz, int interactions, int precision,
+                  double alpha, double beta, double dt, double npart);
+/* gpe_destroy_engine (dev/gpe_engine.cu:370) */
+int gpe_gb_destroy(gpe_gb_engine* e);
+/* gpe_get_lattice (dev/gpe_engine.cu:116) */
+int gpe_gb_get_lattice(const gpe_gb_engine* e, int* nx, int* ny, int* nz);
+/* gpe_change_alpha_beta (dev/gpe_engine.cu:389) */
+int gpe_gb_change_alpha_beta(gpe_gb_engine* e, double alpha, double beta);
+/* gpe_set_time (dev/gpe_engine.cu:417) */
+int gpe_gb_set_time(gpe_gb_engine* e, double t0);
+/* gpe_set_user_params (dev/gpe_engine.cu:426): copies `size` values, zero-fills the rest */
+int gpe_gb_set_user_params(gpe_gb_engine* e, int size, const double* params);
+/* gpe_set_quantum_friction_coeff (dev/gpe_engine.cu:435) */
+int gpe_gb_set_quantum_friction_coeff(gpe_gb_engine* e, double qfcoeff);
+/* gpe_set_psi (dev/gpe_engine.cu:694): psi = 2*nx*ny*nz doubles */
+int gpe_gb_set_psi(gpe_gb_engine* e, double t, const double* psi);
+/* gpe_get_psi (dev/gpe_engine.cu:705) */
+int gpe_gb_get_psi(gpe_gb_engine* e, double* t, double* psi);
+/* gpe_get_density (dev/gpe_engine.cu:669): density = nx*ny*nz doubles */
+int gpe_gb_get_density(gpe_gb_engine* e, double* t, double* density);
+/* gpe_get_norm (dev/gpe_engine.cu:679) */
+int gpe_gb_get_norm(gpe_gb_engine* e, double* norm);
+/* gpe_normalize_psi (dev/gpe_engine.cu:648) */
+int gpe_gb_normalize_psi(gpe_gb_engine* e);
+/* gpe_evolve_qf (dev/gpe_engine.cu:1030); chemical_potential may be NULL */
+int gpe_gb_evolve_qf(gpe_gb_engine* e, int nt, double* chemical_potential);
+/* gpe_energy (dev/gpe_engine.cu:1669) */
+int gpe_gb_energy(gpe_gb_engine* e, double* t, double* ekin, double* eint, double* eext);
+
+/* Device-resident I/O (no reference counterpart; used when the caller keeps
+ * the wavefunction in GPU memory): psi is a device pointer to nx*ny*nz
+ * complex128 values. */
+int gpe_gb_set_psi_device(gpe_gb_engine* e, double t, const void* psi);
+int gpe_gb_get_psi_device(gpe_gb_engine* e, double* t, void* psi);
+/* The CUDA stream (cudaStream_t) this engine launches on, for callers that
+ * order their own work or events against it. */
+void* gpe_gb_get_stream(const gpe_gb_engine* e);
+/* Runs all queued work to completion. */
+int gpe_gb_synchronize(gpe_gb_engine* e);
+/* Number of kernels this engine has launched so far. */
+long long gpe_gb_kernel_launches(const gpe_gb_engine* e);
+/* 1 to replay each step from a captured CUDA graph (default), 0 to launch directly. */
+int gpe_gb_use_graphs(gpe_gb_engine* e, int enable);
+/* Adds a time-sliced potential: `fields` holds nslices real fields of
+ * nx*ny*nz doubles; step `it` uses slice min(it / steps_per_slice, nslices-1)
+ * on top of the harmonic trap.  NULL removes it. */
+int gpe_gb_set_potential_slices(gpe_gb_engine* e, const double* fields, int nslices, int steps_per_slice);
+/* Message for a return code. */
+const char* gpe_gb_error_string(int code);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

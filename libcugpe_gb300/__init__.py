@@ -1,0 +1,221 @@
+"""GB300-native split-step GPE engine (libcugpe's gpe_evolve_qf path).
+
+Python binding of the C ABI in ``include/gpe_gb300.h`` (``libgpe_gb300.so``,
+built in-tree by ``libcugpe_gb300.build``).  The engine runs only on the GPU:
+if the shared library is missing or no CUDA device is present, every call
+fails with an exception; there is no CPU path.
+
+``Engine`` mirrors the reference engine API (KKobuszewski/libcugpe
+dev/gpe_engine.h:299-552) with the lattice and functional given at run time:
+
+    e = Engine((64, 64, 64), interactions=-1, alpha=0.0, beta=1.0, dt=0.016, npart=1.0)
+    e.set_user_params([wx, wy, wz, a_scat])
+    e.set_psi(0.0, psi)          # complex128 [nx, ny, nz]
+    mu = e.evolve_qf(2000)
+    t, ekin, eint, eext = e.energy()
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libgpe_gb300.so")
+
+FP64 = 0
+FP32 = 1
+
+ERR_TOO_MANY_PARAMS = -9
+ERR_LATTICE = -10
+ERR_NO_ENGINE = -11
+ERR_ARGUMENT = -12
+ERR_FUNCTIONAL = -13
+ERR_NOT_IMPLEMENTED = -98
+
+# entry points declared in include/gpe_gb300.h
+C_ABI_SYMBOLS = [
+    "gpe_gb_create", "gpe_gb_destroy", "gpe_gb_get_lattice", "gpe_gb_change_alpha_beta", "gpe_gb_set_time",
+    "gpe_gb_set_user_params", "gpe_gb_set_quantum_friction_coeff", "gpe_gb_set_psi", "gpe_gb_get_psi",
+    "gpe_gb_get_density", "gpe_gb_get_norm", "gpe_gb_normalize_psi", "gpe_gb_evolve_qf", "gpe_gb_energy",
+    "gpe_gb_set_psi_device", "gpe_gb_get_psi_device", "gpe_gb_synchronize", "gpe_gb_kernel_launches",
+    "gpe_gb_use_graphs", "gpe_gb_set_potential_slices", "gpe_gb_error_string", "gpe_gb_get_stream",
+]
+
+
+class GPEError(RuntimeError):
+    def __init__(self, code: int, where: str):
+        self.code = code
+        msg = _lib().gpe_gb_error_string(code).decode() if _LIB is not None else str(code)
+        super().__init__(f"{where} failed with code {code}: {msg}")
+
+
+_LIB = None
+
+
+def _lib():
+    global _LIB
+    if _LIB is None:
+        if not os.path.isfile(LIB_PATH):
+            raise ImportError(f"libgpe_gb300.so not built ({LIB_PATH}); run libcugpe_gb300.build.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, d, i = ctypes.c_void_p, ctypes.c_double, ctypes.c_int
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int)
+        sig = {
+            "gpe_gb_create": (i, [ctypes.POINTER(vp), i, i, i, i, i, d, d, d, d]),
+            "gpe_gb_destroy": (i, [vp]),
+            "gpe_gb_get_lattice": (i, [vp, ip, ip, ip]),
+            "gpe_gb_change_alpha_beta": (i, [vp, d, d]),
+            "gpe_gb_set_time": (i, [vp, d]),
+            "gpe_gb_set_user_params": (i, [vp, i, dp]),
+            "gpe_gb_set_quantum_friction_coeff": (i, [vp, d]),
+            "gpe_gb_set_psi": (i, [vp, d, dp]),
+            "gpe_gb_get_psi": (i, [vp, dp, dp]),
+            "gpe_gb_get_density": (i, [vp, dp, dp]),
+            "gpe_gb_get_norm": (i, [vp, dp]),
+            "gpe_gb_normalize_psi": (i, [vp]),
+            "gpe_gb_evolve_qf": (i, [vp, i, dp]),
+            "gpe_gb_energy": (i, [vp, dp, dp, dp, dp]),
+            "gpe_gb_set_psi_device": (i, [vp, d, vp]),
+            "gpe_gb_get_psi_device": (i, [vp, dp, vp]),
+            "gpe_gb_synchronize": (i, [vp]),
+            "gpe_gb_kernel_launches": (ctypes.c_longlong, [vp]),
+            "gpe_gb_use_graphs": (i, [vp, i]),
+            "gpe_gb_set_potential_slices": (i, [vp, dp, i, i]),
+            "gpe_gb_error_string": (ctypes.c_char_p, [i]),
+            "gpe_gb_get_stream": (vp, [vp]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def lib_path() -> str:
+    return LIB_PATH
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _check(rc: int, where: str):
+    if rc != 0:
+        raise GPEError(rc, where)
+
+
+class Engine:
+    """One condensate on the GPU; the methods follow the reference API."""
+
+    def __init__(self, shape, interactions=-1, alpha=0.0, beta=1.0, dt=1e-3, npart=1.0, precision=FP64):
+        self.shape = tuple(int(s) for s in shape)
+        self.precision = precision
+        self.alpha, self.beta, self.dt, self.npart = alpha, beta, dt, npart
+        L = _lib()
+        h = ctypes.c_void_p()
+        _check(L.gpe_gb_create(ctypes.byref(h), *self.shape, int(interactions), int(precision),
+                               float(alpha), float(beta), float(dt), float(npart)), "gpe_gb_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib().gpe_gb_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_user_params(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        _check(_lib().gpe_gb_set_user_params(self._h, len(p), _dp(p)), "set_user_params")
+
+    def change_alpha_beta(self, alpha, beta):
+        self.alpha, self.beta = alpha, beta
+        _check(_lib().gpe_gb_change_alpha_beta(self._h, float(alpha), float(beta)), "change_alpha_beta")
+
+    def set_rte_evolution(self):
+        self.change_alpha_beta(1.0, 0.0)
+
+    def set_ite_evolution(self):
+        self.change_alpha_beta(0.0, 1.0)
+
+    def set_time(self, t0):
+        _check(_lib().gpe_gb_set_time(self._h, float(t0)), "set_time")
+
+    def set_quantum_friction_coeff(self, q):
+        _check(_lib().gpe_gb_set_quantum_friction_coeff(self._h, float(q)), "set_quantum_friction_coeff")
+
+    def set_psi(self, t, psi):
+        p = np.ascontiguousarray(psi, dtype=np.complex128).reshape(self.shape)
+        _check(_lib().gpe_gb_set_psi(self._h, float(t), _dp(p.view(np.float64))), "set_psi")
+
+    def get_psi(self, out=None):
+        out = np.empty(self.shape, dtype=np.complex128) if out is None else out
+        t = ctypes.c_double()
+        _check(_lib().gpe_gb_get_psi(self._h, ctypes.byref(t), _dp(out.view(np.float64))), "get_psi")
+        return t.value, out
+
+    def set_psi_device(self, t, ptr: int):
+        _check(_lib().gpe_gb_set_psi_device(self._h, float(t), ctypes.c_void_p(ptr)), "set_psi_device")
+
+    def get_psi_device(self, ptr: int):
+        t = ctypes.c_double()
+        _check(_lib().gpe_gb_get_psi_device(self._h, ctypes.byref(t), ctypes.c_void_p(ptr)), "get_psi_device")
+        return t.value
+
+    def get_density(self):
+        out = np.empty(self.shape, dtype=np.float64)
+        t = ctypes.c_double()
+        _check(_lib().gpe_gb_get_density(self._h, ctypes.byref(t), _dp(out)), "get_density")
+        return t.value, out
+
+    def get_norm(self):
+        n = ctypes.c_double()
+        _check(_lib().gpe_gb_get_norm(self._h, ctypes.byref(n)), "get_norm")
+        return n.value
+
+    def normalize_psi(self):
+        _check(_lib().gpe_gb_normalize_psi(self._h), "normalize_psi")
+
+    def evolve_qf(self, nt):
+        mu = ctypes.c_double(0.0)
+        _check(_lib().gpe_gb_evolve_qf(self._h, int(nt), ctypes.byref(mu)), "evolve_qf")
+        return mu.value
+
+    def energy(self):
+        t, a, b, c = (ctypes.c_double() for _ in range(4))
+        _check(_lib().gpe_gb_energy(self._h, ctypes.byref(t), ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
+               "energy")
+        return t.value, a.value, b.value, c.value
+
+    def synchronize(self):
+        _check(_lib().gpe_gb_synchronize(self._h), "synchronize")
+
+    def stream_handle(self) -> int:
+        return int(_lib().gpe_gb_get_stream(self._h) or 0)
+
+    def kernel_launches(self) -> int:
+        return int(_lib().gpe_gb_kernel_launches(self._h))
+
+    def use_graphs(self, enable: bool):
+        _check(_lib().gpe_gb_use_graphs(self._h, 1 if enable else 0), "use_graphs")
+
+    def set_potential_slices(self, fields, steps_per_slice):
+        if fields is None:
+            _check(_lib().gpe_gb_set_potential_slices(self._h, None, 0, 0), "set_potential_slices")
+            return
+        f = np.ascontiguousarray(fields, dtype=np.float64)
+        self._slices = f
+        _check(_lib().gpe_gb_set_potential_slices(self._h, _dp(f), f.shape[0], int(steps_per_slice)),
+               "set_potential_slices")

@@ -1,0 +1,792 @@
+// GB300 split-step GPE engine: state, tables, the step schedule, reductions
+// and both API layers (handle-based C ABI and the reference's global-engine
+// C++ API).
+//
+// The step is the reference's predictor-corrector Strang step
+// (dev/gpe_engine.cu:1030-1109), applied as fused pencil passes:
+//
+//   plain step (no quantum friction), 6 passes:
+//     z: psi -> [Vstep1] -> Kz -> psi2          (also stores V)
+//     y: psi2 -> Ky -> psi2
+//     x: psi2 -> Kx -> RTE: [Vstep2] -> psi     ITE: [part1] -> psi2, sum rho
+//     z: psi -> ITE: [part2 with psi2 * s2] -> Kz -> psi
+//     y: psi -> Ky -> psi
+//     x: psi -> Kx -> [Vstep3] -> psi           ITE: sum rho -> s_prev, mu
+//   quantum friction adds the spectral Laplacian, computed once per step
+//   (the reference computes it twice on the same psi, :1040 and :1074):
+//     z: lap = Dz psi;  y: lap += Dy psi;  x: lap += Dx psi -> V_qf, Vstep1_qf
+//        -> Kx -> psi2;  z: Kz psi2;  y: Ky psi2 -> [part1 (+part2)] ...
+//
+// ITE normalisation of psi is applied lazily: the last pass publishes the
+// factor s_prev = sqrt(npart / sum) and the next step multiplies psi by it
+// when it reads psi (bit-identical to scaling in place first).  The factor
+// is applied to the stored psi when evolve returns.  mu stays on the device
+// and is read once at the end (the reference copies it back every step).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#include <limits.h>
+#include <new>
+#include <vector>
+
+#include "gpe_launch.cuh"
+#include "../../include/gpe_gb300.h"
+
+namespace gpe {
+
+// ------------------------------------------------------------ utility kernels
+
+template <typename R>
+__global__ void k_apply_scale(C2<R>* p, size_t n, const DynState* d) {
+    const R s = (R)d->s_prev;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        p[i] = cscale(p[i], s);
+}
+
+template <typename R>
+__global__ void k_apply_norm(C2<R>* p, size_t n, const DynState* d, int slot, double npart) {
+    const R s = (R)sqrt(npart / d->red[slot]);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        p[i] = cscale(p[i], s);
+}
+
+__global__ void k_set_state(DynState* d, unsigned it, double s_prev) {
+    d->it = it;
+    d->s_prev = s_prev;
+    d->s2 = 1.0;
+    d->ticket = 0;
+}
+
+__global__ void k_reset_scale(DynState* d) { d->s_prev = 1.0; }
+
+template <typename R>
+__global__ void k_to_double(const C2<R>* in, double2* out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = make_double2((double)in[i].x, (double)in[i].y);
+}
+
+template <typename R>
+__global__ void k_from_double(const double2* in, C2<R>* out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        C2<R> v; v.x = (R)in[i].x; v.y = (R)in[i].y; out[i] = v;
+    }
+}
+
+template <typename R>
+__global__ void k_density(const C2<R>* in, double* out, size_t n, double gamma) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double x = in[i].x, y = in[i].y;
+        out[i] = gamma * (x * x + y * y);
+    }
+}
+
+// sum of Gamma |psi|^2 -> d->red[slot]; fixed grid, deterministic order
+constexpr int kRedThreads = 256;
+constexpr int kRedBlocks = 1024;
+
+template <typename R>
+__global__ void __launch_bounds__(kRedThreads) k_norm(const C2<R>* in, size_t n, double gamma, double* partials,
+                                                      DynState* d, int slot) {
+    __shared__ double sw[kRedThreads / 32];
+    __shared__ bool last;
+    double acc = 0.0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double x = in[i].x, y = in[i].y;
+        acc += gamma * (x * x + y * y);
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < kRedThreads / 32; w++) s += sw[w];
+        partials[blockIdx.x] = s;
+        __threadfence();
+        last = (atomicAdd(&d->ticket, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        double s = 0.0, c = 0.0;
+        for (unsigned b = 0; b < gridDim.x; b++) {
+            const double x = __ldcg(partials + b);
+            const double t = s + x;
+            c += (fabs(s) >= fabs(x)) ? (s - t) + x : (x - t) + s;
+            s = t;
+        }
+        d->red[slot] = s + c;
+        d->ticket = 0;
+        __threadfence();
+    }
+}
+
+// --------------------------------------------------------------- the engine
+
+struct AxisTables {
+    void* ktab;   // C2<R>[N]  exp(c3 k^2 / Gamma^2) / N
+    void* lqf;    // R[N]      (qf / Gamma) k^2 / N
+    void* lek;    // R[N]      k^2 / (2 Gamma) / N
+    void* tw;     // C2<R>[N]  exp(-2 pi i p / N)
+    void* vt;     // R[N]      0.5 i^2 w^2, i = index - N/2
+};
+
+struct Engine {
+    int n3[3];
+    int l3[3];
+    size_t n = 0;
+    int inter = 0;
+    double gamma = 1.0;
+    int prec = GPE_PRECISION_FP64;
+    double alpha = 0, beta = 0, dt = 0, npart = 1, t0 = 0, qf_raw = 0;
+    unsigned it = 0;
+    double up[32] = {0};
+    cudaStream_t st = nullptr;
+
+    void *psi = nullptr, *psi2 = nullptr, *lap = nullptr, *aux = nullptr, *V = nullptr, *Vqf = nullptr;
+    DynState* dyn = nullptr;
+    double* partials = nullptr;
+    void* tabmem = nullptr;
+    AxisTables ax[3];
+    double2* stage = nullptr;  // FP64 staging for host I/O of the FP32 form
+    double* dens = nullptr;
+    void* vextra = nullptr;
+    int vslices = 0, vsteps = 1;
+
+    bool use_graph = true;
+    bool graph_dirty = true;
+    cudaGraphExec_t gexec = nullptr;
+    int gsteps = 0;
+    int passes_per_step = 0;
+    long long launches = 0;
+
+    size_t rsize() const { return prec == GPE_PRECISION_FP32 ? sizeof(float) : sizeof(double); }
+    size_t csize() const { return 2 * rsize(); }
+};
+
+static int cuda_rc(cudaError_t e) { return e == cudaSuccess ? 0 : (int)e; }
+#define GPE_CK(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) return (int)_e; } while (0)
+#define GPE_RC(x) do { int _r = (x); if (_r) return _r; } while (0)
+
+static void util_grid(size_t n, int* blocks, int* threads) {
+    *threads = 256;
+    size_t b = (n + 255) / 256;
+    if (b > 4096) b = 4096;
+    *blocks = (int)(b > 0 ? b : 1);
+}
+
+static void kgrid(std::vector<double>& k, int n) {
+    // dev/gpe_engine.cu:147-154
+    k.resize(n);
+    int i, j;
+    for (i = 0; i <= n / 2 - 1; i++) k[i] = 2. * M_PI / n * (double)i;
+    j = -i;
+    for (i = n / 2; i < n; i++) { k[i] = 2. * M_PI / n * (double)j; j++; }
+}
+
+static void step_coeff(const Engine* e, double* c3x, double* c3y) {
+    // c3 = Gamma * 0.5 * dt / (-beta + i alpha)   (dev/gpe_engine.cu:177-181)
+    const double a = e->gamma * 0.5 * e->dt;
+    const double br = -1.0 * e->beta, bi = e->alpha;
+    const double den = br * br + bi * bi;
+    *c3x = a * br / den;
+    *c3y = -a * bi / den;
+}
+
+template <typename R>
+static int upload_tables(Engine* e) {
+    double c3x, c3y;
+    step_coeff(e, &c3x, &c3y);
+    const double g2 = e->gamma * e->gamma;
+    size_t off = 0;
+    std::vector<unsigned char> host;
+    size_t total = 0;
+    for (int a = 0; a < 3; a++) total += (size_t)e->n3[a] * (2 * sizeof(C2<R>) + 3 * sizeof(R)) + 256 * 5;
+    host.assign(total, 0);
+    if (!e->tabmem) GPE_CK(cudaMalloc(&e->tabmem, total));
+    unsigned char* dbase = (unsigned char*)e->tabmem;
+    auto take = [&](size_t bytes) { off = (off + 255) & ~(size_t)255; size_t o = off; off += bytes; return o; };
+    for (int a = 0; a < 3; a++) {
+        const int N = e->n3[a];
+        std::vector<double> k;
+        kgrid(k, N);
+        const size_t okt = take(N * sizeof(C2<R>)), olq = take(N * sizeof(R)), ole = take(N * sizeof(R)),
+                     otw = take(N * sizeof(C2<R>)), ovt = take(N * sizeof(R));
+        C2<R>* kt = (C2<R>*)(host.data() + okt);
+        R* lq = (R*)(host.data() + olq);
+        R* le = (R*)(host.data() + ole);
+        C2<R>* tw = (C2<R>*)(host.data() + otw);
+        R* vt = (R*)(host.data() + ovt);
+        const double w = e->up[a];
+        for (int i = 0; i < N; i++) {
+            // exp(c3 k^2 / Gamma^2) (dev/gpe_engine.cu:186-216), with 1/N_a of the unnormalised inverse
+            double zx = c3x * k[i], zy = c3y * k[i];
+            zx *= k[i]; zy *= k[i];
+            zx /= g2; zy /= g2;
+            const double ex = exp(zx);
+            kt[i].x = (R)(ex * cos(zy) / (double)N);
+            kt[i].y = (R)(ex * sin(zy) / (double)N);
+            lq[i] = (R)((e->qf_raw / e->gamma) * (k[i] * k[i]) / (double)N);
+            le[i] = (R)((k[i] * k[i]) / (2.0 * e->gamma) / (double)N);
+            const long double ang = -2.0L * 3.14159265358979323846264338327950288L * (long double)i / (long double)N;
+            tw[i].x = (R)(double)cosl(ang);
+            tw[i].y = (R)(double)sinl(ang);
+            const double ii = (double)i - 1.0 * (N / 2);
+            vt[i] = (R)(0.5 * ii * ii * w * w);  // dev/gpe_user_defined.h:500-510
+        }
+        e->ax[a].ktab = dbase + okt; e->ax[a].lqf = dbase + olq; e->ax[a].lek = dbase + ole;
+        e->ax[a].tw = dbase + otw; e->ax[a].vt = dbase + ovt;
+    }
+    GPE_CK(cudaMemcpyAsync(e->tabmem, host.data(), off, cudaMemcpyHostToDevice, e->st));
+    GPE_CK(cudaStreamSynchronize(e->st));
+    e->graph_dirty = true;
+    return 0;
+}
+
+static int upload(Engine* e) {
+    return e->prec == GPE_PRECISION_FP32 ? upload_tables<float>(e) : upload_tables<double>(e);
+}
+
+template <typename R>
+static Phys<R> make_phys(const Engine* e) {
+    Phys<R> p;
+    double c3x, c3y;
+    step_coeff(e, &c3x, &c3y);
+    p.inter = e->inter;
+    p.phase_mode = (c3x == 0.0) ? PHASE_ROTATE : (c3y == 0.0) ? PHASE_DECAY : PHASE_GENERAL;
+    p.gamma = (R)e->gamma;
+    p.c3x = (R)c3x;
+    p.c3y = (R)c3y;
+    p.c_bec = (R)(4 * M_PI * e->up[3]);
+    p.a_scat = (R)e->up[3];
+    p.qf_eps = (R)1.0e-12;
+    return p;
+}
+
+struct PassDesc {
+    int axis;
+    int pre, mid, post;
+    uint32_t flags;
+    int in, out;  // buffer ids
+};
+enum { B_NONE = 0, B_PSI = 1, B_PSI2 = 2 };
+
+// The reference step sequence (dev/gpe_engine.cu:1035-1106) as fused passes.
+static std::vector<PassDesc> schedule(const Engine* e) {
+    std::vector<PassDesc> s;
+    const bool ite = e->beta != 0.0;
+    const bool qf = e->qf_raw != 0.0;
+    const uint32_t aux = (e->prec == GPE_PRECISION_FP64) ? F_AUX_CPLX : 0u;
+    const uint32_t sin_ = ite ? F_SCALE_IN : 0u;
+    if (!qf) {
+        s.push_back({AX_Z, PRE_VSTEP1, MID_NONE, POST_NONE, F_KIN | F_STORE | sin_, B_PSI, B_PSI2});
+        s.push_back({AX_Y, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI2, B_PSI2});
+        if (!ite) {
+            s.push_back({AX_X, PRE_NONE, MID_NONE, POST_VSTEP2, F_KIN | F_STORE | aux, B_PSI2, B_PSI});
+            s.push_back({AX_Z, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
+            s.push_back({AX_Y, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
+            s.push_back({AX_X, PRE_NONE, MID_NONE, POST_VSTEP3, F_KIN | F_STORE | aux | F_FIN_STEP, B_PSI, B_PSI});
+        } else {
+            s.push_back({AX_X, PRE_NONE, MID_NONE, POST_PART1, F_KIN | F_STORE | F_REDUCE | F_FIN_S2, B_PSI2, B_PSI2});
+            s.push_back({AX_Z, PRE_PART2, MID_NONE, POST_NONE, F_KIN | F_STORE | F_SCALE_IN | F_SCALE_PSI2 | aux,
+                         B_PSI, B_PSI});
+            s.push_back({AX_Y, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
+            s.push_back({AX_X, PRE_NONE, MID_NONE, POST_VSTEP3, F_KIN | F_STORE | aux | F_REDUCE | F_FIN_STEP, B_PSI,
+                         B_PSI});
+        }
+    } else {
+        s.push_back({AX_Z, PRE_NONE, MID_LAP_STORE, POST_NONE, F_LAP | sin_, B_PSI, B_NONE});
+        s.push_back({AX_Y, PRE_NONE, MID_LAP_ACC, POST_NONE, F_LAP | sin_, B_PSI, B_NONE});
+        s.push_back({AX_X, PRE_NONE, MID_QF_VSTEP1, POST_NONE, F_LAP | F_KIN | F_STORE | sin_, B_PSI, B_PSI2});
+        s.push_back({AX_Z, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI2, B_PSI2});
+        if (!ite) {
+            s.push_back({AX_Y, PRE_NONE, MID_NONE, POST_PART12, F_KIN | F_STORE | F_QF | aux, B_PSI2, B_PSI});
+            s.push_back({AX_X, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
+            s.push_back({AX_Z, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
+            s.push_back({AX_Y, PRE_NONE, MID_NONE, POST_VSTEP3, F_KIN | F_STORE | aux | F_FIN_STEP, B_PSI, B_PSI});
+        } else {
+            s.push_back({AX_Y, PRE_NONE, MID_NONE, POST_PART1, F_KIN | F_STORE | F_REDUCE | F_FIN_S2, B_PSI2, B_PSI2});
+            s.push_back({AX_X, PRE_PART2, MID_NONE, POST_NONE,
+                         F_KIN | F_STORE | F_SCALE_IN | F_SCALE_PSI2 | F_QF | aux, B_PSI, B_PSI});
+            s.push_back({AX_Z, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
+            s.push_back({AX_Y, PRE_NONE, MID_NONE, POST_VSTEP3, F_KIN | F_STORE | aux | F_REDUCE | F_FIN_STEP, B_PSI,
+                         B_PSI});
+        }
+    }
+    return s;
+}
+
+template <typename R>
+static PassArgs<R> base_args(const Engine* e) {
+    PassArgs<R> a;
+    memset(&a, 0, sizeof a);
+    a.psi = (C2<R>*)e->psi;
+    a.psi2 = (const C2<R>*)e->psi2;
+    a.lap = (C2<R>*)e->lap;
+    a.aux = e->aux;
+    a.V = (R*)e->V;
+    a.Vqf = (R*)e->Vqf;
+    a.vx = (const R*)e->ax[0].vt;
+    a.vy = (const R*)e->ax[1].vt;
+    a.vz = (const R*)e->ax[2].vt;
+    a.vextra = (const R*)e->vextra;
+    a.vsteps = e->vsteps;
+    a.vslices = e->vslices;
+    a.dyn = e->dyn;
+    a.partials = e->partials;
+    a.lx = e->l3[0]; a.ly = e->l3[1]; a.lz = e->l3[2];
+    a.npart = e->npart;
+    a.dt = e->dt;
+    a.ph = make_phys<R>(e);
+    return a;
+}
+
+template <typename R>
+static void axis_args(const Engine* e, PassArgs<R>& a, int axis) {
+    a.ktab = (const C2<R>*)e->ax[axis].ktab;
+    a.tw = (const C2<R>*)e->ax[axis].tw;
+}
+
+static size_t pencils_of(const Engine* e, int axis) { return e->n / (size_t)e->n3[axis]; }
+
+template <typename R>
+static int launch_desc(Engine* e, const PassDesc& d) {
+    PassArgs<R> a = base_args<R>(e);
+    axis_args(e, a, d.axis);
+    a.ltab = (const R*)e->ax[d.axis].lqf;
+    a.in = (const C2<R>*)(d.in == B_PSI ? e->psi : e->psi2);
+    a.out = (C2<R>*)(d.out == B_PSI ? e->psi : d.out == B_PSI2 ? e->psi2 : nullptr);
+    a.pre = d.pre; a.mid = d.mid; a.post = d.post;
+    a.flags = d.flags | (e->vextra ? F_VEXTRA : 0u);
+    e->launches++;
+    return cuda_rc(launch_pass<R>(a, e->n3[d.axis], d.axis, pencils_of(e, d.axis), e->st));
+}
+
+template <typename R>
+static int run_step(Engine* e, const std::vector<PassDesc>& s) {
+    for (const PassDesc& d : s) GPE_RC(launch_desc<R>(e, d));
+    return 0;
+}
+
+static int run_steps(Engine* e, const std::vector<PassDesc>& s, int k) {
+    for (int i = 0; i < k; i++)
+        GPE_RC(e->prec == GPE_PRECISION_FP32 ? run_step<float>(e, s) : run_step<double>(e, s));
+    return 0;
+}
+
+static void drop_graph(Engine* e) {
+    if (e->gexec) cudaGraphExecDestroy(e->gexec);
+    e->gexec = nullptr;
+    e->gsteps = 0;
+}
+
+static int build_graph(Engine* e, const std::vector<PassDesc>& s, int k) {
+    drop_graph(e);
+    cudaGraph_t g = nullptr;
+    GPE_CK(cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal));
+    const long long before = e->launches;
+    int rc = run_steps(e, s, k);
+    e->launches = before;  // counted when the graph is replayed
+    cudaError_t ce = cudaStreamEndCapture(e->st, &g);
+    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+    GPE_CK(ce);
+    ce = cudaGraphInstantiate(&e->gexec, g, 0);
+    cudaGraphDestroy(g);
+    GPE_CK(ce);
+    e->gsteps = k;
+    e->graph_dirty = false;
+    return 0;
+}
+
+static int set_state(Engine* e, unsigned it, double s_prev) {
+    k_set_state<<<1, 1, 0, e->st>>>(e->dyn, it, s_prev);
+    e->launches++;
+    return cuda_rc(cudaGetLastError());
+}
+
+template <typename R>
+static int finish_ite(Engine* e) {
+    int b, t;
+    util_grid(e->n, &b, &t);
+    k_apply_scale<R><<<b, t, 0, e->st>>>((C2<R>*)e->psi, e->n, e->dyn);
+    k_reset_scale<<<1, 1, 0, e->st>>>(e->dyn);
+    e->launches += 2;
+    return cuda_rc(cudaGetLastError());
+}
+
+static const int kGraphSteps = 16;
+
+static int evolve(Engine* e, int nt, double* mu) {
+    if (nt <= 0) return 0;
+    const std::vector<PassDesc> s = schedule(e);
+    e->passes_per_step = (int)s.size();
+    int done = 0;
+    if (e->use_graph) {
+        // first steps run directly: this also configures every kernel outside capture
+        if (e->graph_dirty || !e->gexec) {
+            GPE_RC(run_steps(e, s, 1));
+            done = 1;
+            if (nt - done >= 2) GPE_RC(build_graph(e, s, nt - done < kGraphSteps ? nt - done : kGraphSteps));
+        }
+        while (e->gexec && nt - done >= e->gsteps) {
+            GPE_CK(cudaGraphLaunch(e->gexec, e->st));
+            e->launches += (long long)e->gsteps * e->passes_per_step;
+            done += e->gsteps;
+        }
+    }
+    GPE_RC(run_steps(e, s, nt - done));
+    if (e->beta != 0.0) {
+        GPE_RC(e->prec == GPE_PRECISION_FP32 ? finish_ite<float>(e) : finish_ite<double>(e));
+        if (mu) {
+            double m = 0.0;
+            GPE_CK(cudaMemcpyAsync(&m, &e->dyn->mu, sizeof(double), cudaMemcpyDeviceToHost, e->st));
+            GPE_CK(cudaStreamSynchronize(e->st));
+            *mu = m;
+        }
+    }
+    e->it += (unsigned)nt;
+    return cuda_rc(cudaGetLastError());
+}
+
+template <typename R>
+static int norm_to_slot(Engine* e, int slot) {
+    k_norm<R><<<kRedBlocks, kRedThreads, 0, e->st>>>((const C2<R>*)e->psi, e->n, e->gamma, e->partials, e->dyn, slot);
+    e->launches++;
+    return cuda_rc(cudaGetLastError());
+}
+
+template <typename R>
+static int normalize_psi(Engine* e) {
+    GPE_RC(norm_to_slot<R>(e, 12));
+    int b, t;
+    util_grid(e->n, &b, &t);
+    k_apply_norm<R><<<b, t, 0, e->st>>>((C2<R>*)e->psi, e->n, e->dyn, 12, e->npart);
+    e->launches++;
+    return cuda_rc(cudaGetLastError());
+}
+
+template <typename R>
+static int energy(Engine* e, double* ekin, double* eint, double* eext) {
+    if (e->beta == 0.0) GPE_RC(normalize_psi<R>(e));  // dev/gpe_engine.cu:1676-1680
+    const int order[3] = {AX_Z, AX_Y, AX_X};
+    for (int i = 0; i < 3; i++) {
+        const int axis = order[i];
+        PassArgs<R> a = base_args<R>(e);
+        axis_args(e, a, axis);
+        a.ltab = (const R*)e->ax[axis].lek;
+        a.in = (const C2<R>*)e->psi;
+        a.out = nullptr;
+        a.pre = (axis == AX_Z) ? PRE_ENERGY : PRE_NONE;
+        a.mid = MID_NONE;
+        a.post = POST_NONE;
+        a.flags = F_EKIN | F_FIN_RED | (e->vextra ? F_VEXTRA : 0u);
+        a.red_slot = 3 * i;
+        e->launches++;
+        GPE_RC(cuda_rc(launch_pass<R>(a, e->n3[axis], axis, pencils_of(e, axis), e->st)));
+    }
+    double red[9];
+    GPE_CK(cudaMemcpyAsync(red, e->dyn->red, sizeof red, cudaMemcpyDeviceToHost, e->st));
+    GPE_CK(cudaStreamSynchronize(e->st));
+    *eext = red[0];
+    *eint = red[1];
+    *ekin = (red[2] + red[5]) + red[8];
+    return 0;
+}
+
+static size_t max_grid(const Engine* e) {
+    size_t g = kRedBlocks;
+    for (int a = 0; a < 3; a++) {
+        const size_t p = pass_grid(e->n3[a], pencils_of(e, a));
+        if (p > g) g = p;
+    }
+    return g;
+}
+
+static void release(Engine* e) {
+    drop_graph(e);
+    cudaFree(e->psi); cudaFree(e->psi2); cudaFree(e->lap); cudaFree(e->aux); cudaFree(e->V); cudaFree(e->Vqf);
+    cudaFree(e->dyn); cudaFree(e->partials); cudaFree(e->tabmem); cudaFree(e->stage); cudaFree(e->dens);
+    cudaFree(e->vextra);
+    if (e->st) cudaStreamDestroy(e->st);
+}
+
+static bool pow2_side(int v) { return v >= 8 && v <= 512 && (v & (v - 1)) == 0; }
+
+}  // namespace gpe
+
+using gpe::Engine;
+
+// ===================================================================== C ABI
+
+struct gpe_gb_engine {
+    Engine e;
+};
+
+extern "C" {
+
+int gpe_gb_create(gpe_gb_engine** out, int nx, int ny, int nz, int interactions, int precision, double alpha,
+                  double beta, double dt, double npart) {
+    if (!out) return GPE_ERR_ARGUMENT;
+    *out = nullptr;
+    if (!gpe::pow2_side(nx) || !gpe::pow2_side(ny) || !gpe::pow2_side(nz)) return GPE_ERR_LATTICE;
+    if (interactions < -1 || interactions > 1) return GPE_ERR_FUNCTIONAL;
+    if (precision != GPE_PRECISION_FP64 && precision != GPE_PRECISION_FP32) return GPE_ERR_ARGUMENT;
+    gpe_gb_engine* h = new (std::nothrow) gpe_gb_engine();
+    if (!h) return GPE_ERR_ARGUMENT;
+    Engine* e = &h->e;
+    e->n3[0] = nx; e->n3[1] = ny; e->n3[2] = nz;
+    for (int a = 0; a < 3; a++) e->l3[a] = __builtin_ctz((unsigned)e->n3[a]);
+    e->n = (size_t)nx * ny * nz;
+    e->inter = interactions;
+    e->gamma = (interactions == -1) ? 1.0 : 2.0;  // GPE_FOR defaults, dev/gpe_user_defined.h:104,182,289
+    e->prec = precision;
+    e->alpha = alpha; e->beta = beta; e->dt = dt; e->npart = npart;
+    const size_t cs = e->csize(), rs = e->rsize();
+    int rc = 0;
+    cudaError_t ce;
+    if ((ce = cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking)) != cudaSuccess) rc = (int)ce;
+    if (!rc && (ce = cudaMalloc(&e->psi, cs * e->n)) != cudaSuccess) rc = (int)ce;
+    if (!rc && (ce = cudaMalloc(&e->psi2, cs * e->n)) != cudaSuccess) rc = (int)ce;
+    if (!rc && (ce = cudaMalloc(&e->aux, (precision == GPE_PRECISION_FP64 ? cs : rs) * e->n)) != cudaSuccess) rc = (int)ce;
+    if (!rc && (ce = cudaMalloc(&e->V, rs * e->n)) != cudaSuccess) rc = (int)ce;
+    if (!rc && (ce = cudaMalloc(&e->dyn, sizeof(gpe::DynState))) != cudaSuccess) rc = (int)ce;
+    if (!rc && (ce = cudaMalloc(&e->partials, sizeof(double) * gpe::NRED * gpe::max_grid(e))) != cudaSuccess) rc = (int)ce;
+    if (!rc && (ce = cudaMemsetAsync(e->psi, 0, cs * e->n, e->st)) != cudaSuccess) rc = (int)ce;
+    if (!rc && (ce = cudaMemsetAsync(e->dyn, 0, sizeof(gpe::DynState), e->st)) != cudaSuccess) rc = (int)ce;
+    if (!rc) rc = gpe::set_state(e, 0, 1.0);
+    if (!rc) rc = gpe::upload(e);
+    if (rc) {
+        gpe::release(e);
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return 0;
+}
+
+int gpe_gb_destroy(gpe_gb_engine* h) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    cudaStreamSynchronize(h->e.st);
+    gpe::release(&h->e);
+    delete h;
+    return gpe::cuda_rc(cudaGetLastError());
+}
+
+int gpe_gb_get_lattice(const gpe_gb_engine* h, int* nx, int* ny, int* nz) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    if (nx) *nx = h->e.n3[0];
+    if (ny) *ny = h->e.n3[1];
+    if (nz) *nz = h->e.n3[2];
+    return 0;
+}
+
+int gpe_gb_change_alpha_beta(gpe_gb_engine* h, double alpha, double beta) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    h->e.alpha = alpha;
+    h->e.beta = beta;
+    return gpe::upload(&h->e);
+}
+
+int gpe_gb_set_time(gpe_gb_engine* h, double t0) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    Engine* e = &h->e;
+    e->t0 = t0;
+    e->it = 0;
+    // keep a pending ITE scale (none outside evolve) and reset the device step counter
+    GPE_RC(gpe::set_state(e, 0, 1.0));
+    return gpe::cuda_rc(cudaStreamSynchronize(e->st));
+}
+
+int gpe_gb_set_user_params(gpe_gb_engine* h, int size, const double* params) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    if (size > 32) return GPE_ERR_TOO_MANY_PARAMS;
+    if (size < 0 || (size > 0 && !params)) return GPE_ERR_ARGUMENT;
+    memset(h->e.up, 0, sizeof h->e.up);
+    if (size > 0) memcpy(h->e.up, params, sizeof(double) * (size_t)size);
+    return gpe::upload(&h->e);
+}
+
+int gpe_gb_set_quantum_friction_coeff(gpe_gb_engine* h, double q) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    Engine* e = &h->e;
+    e->qf_raw = q;
+    if (q != 0.0) {
+        if (!e->lap) GPE_CK(cudaMalloc(&e->lap, e->csize() * e->n));
+        if (!e->Vqf) GPE_CK(cudaMalloc(&e->Vqf, e->rsize() * e->n));
+    } else {
+        cudaStreamSynchronize(e->st);
+        cudaFree(e->lap); cudaFree(e->Vqf);
+        e->lap = nullptr; e->Vqf = nullptr;
+    }
+    return gpe::upload(e);
+}
+
+static int stage_alloc(Engine* e) {
+    if (!e->stage) GPE_CK(cudaMalloc(&e->stage, sizeof(double2) * e->n));
+    return 0;
+}
+
+static int set_psi_from(Engine* e, double t, const void* src, cudaMemcpyKind kind) {
+    if (e->prec == GPE_PRECISION_FP64) {
+        GPE_CK(cudaMemcpyAsync(e->psi, src, sizeof(double2) * e->n, kind, e->st));
+    } else {
+        GPE_RC(stage_alloc(e));
+        GPE_CK(cudaMemcpyAsync(e->stage, src, sizeof(double2) * e->n, kind, e->st));
+        int b, th;
+        gpe::util_grid(e->n, &b, &th);
+        gpe::k_from_double<float><<<b, th, 0, e->st>>>(e->stage, (float2*)e->psi, e->n);
+        e->launches++;
+        GPE_CK(cudaGetLastError());
+    }
+    e->t0 = t;
+    e->it = 0;
+    GPE_RC(gpe::set_state(e, 0, 1.0));
+    return gpe::cuda_rc(cudaStreamSynchronize(e->st));
+}
+
+static int get_psi_to(Engine* e, double* t, void* dst, cudaMemcpyKind kind) {
+    if (e->prec == GPE_PRECISION_FP64) {
+        GPE_CK(cudaMemcpyAsync(dst, e->psi, sizeof(double2) * e->n, kind, e->st));
+    } else {
+        GPE_RC(stage_alloc(e));
+        int b, th;
+        gpe::util_grid(e->n, &b, &th);
+        gpe::k_to_double<float><<<b, th, 0, e->st>>>((const float2*)e->psi, e->stage, e->n);
+        e->launches++;
+        GPE_CK(cudaGetLastError());
+        GPE_CK(cudaMemcpyAsync(dst, e->stage, sizeof(double2) * e->n, kind, e->st));
+    }
+    GPE_CK(cudaStreamSynchronize(e->st));
+    if (t) *t = e->t0 + e->dt * e->it;
+    return 0;
+}
+
+int gpe_gb_set_psi(gpe_gb_engine* h, double t, const double* psi) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    if (!psi) return GPE_ERR_ARGUMENT;
+    return set_psi_from(&h->e, t, psi, cudaMemcpyHostToDevice);
+}
+
+int gpe_gb_get_psi(gpe_gb_engine* h, double* t, double* psi) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    if (!psi) return GPE_ERR_ARGUMENT;
+    return get_psi_to(&h->e, t, psi, cudaMemcpyDeviceToHost);
+}
+
+int gpe_gb_set_psi_device(gpe_gb_engine* h, double t, const void* psi) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    if (!psi) return GPE_ERR_ARGUMENT;
+    return set_psi_from(&h->e, t, psi, cudaMemcpyDeviceToDevice);
+}
+
+int gpe_gb_get_psi_device(gpe_gb_engine* h, double* t, void* psi) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    if (!psi) return GPE_ERR_ARGUMENT;
+    return get_psi_to(&h->e, t, psi, cudaMemcpyDeviceToDevice);
+}
+
+int gpe_gb_get_density(gpe_gb_engine* h, double* t, double* density) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    if (!density) return GPE_ERR_ARGUMENT;
+    Engine* e = &h->e;
+    if (!e->dens) GPE_CK(cudaMalloc(&e->dens, sizeof(double) * e->n));
+    int b, th;
+    gpe::util_grid(e->n, &b, &th);
+    if (e->prec == GPE_PRECISION_FP32) gpe::k_density<float><<<b, th, 0, e->st>>>((const float2*)e->psi, e->dens, e->n, e->gamma);
+    else gpe::k_density<double><<<b, th, 0, e->st>>>((const double2*)e->psi, e->dens, e->n, e->gamma);
+    e->launches++;
+    GPE_CK(cudaGetLastError());
+    GPE_CK(cudaMemcpyAsync(density, e->dens, sizeof(double) * e->n, cudaMemcpyDeviceToHost, e->st));
+    GPE_CK(cudaStreamSynchronize(e->st));
+    if (t) *t = e->t0 + e->dt * e->it;
+    return 0;
+}
+
+int gpe_gb_get_norm(gpe_gb_engine* h, double* norm) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    if (!norm) return GPE_ERR_ARGUMENT;
+    Engine* e = &h->e;
+    GPE_RC(e->prec == GPE_PRECISION_FP32 ? gpe::norm_to_slot<float>(e, 13) : gpe::norm_to_slot<double>(e, 13));
+    GPE_CK(cudaMemcpyAsync(norm, &e->dyn->red[13], sizeof(double), cudaMemcpyDeviceToHost, e->st));
+    return gpe::cuda_rc(cudaStreamSynchronize(e->st));
+}
+
+int gpe_gb_normalize_psi(gpe_gb_engine* h) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    Engine* e = &h->e;
+    GPE_RC(e->prec == GPE_PRECISION_FP32 ? gpe::normalize_psi<float>(e) : gpe::normalize_psi<double>(e));
+    return gpe::cuda_rc(cudaStreamSynchronize(e->st));
+}
+
+int gpe_gb_evolve_qf(gpe_gb_engine* h, int nt, double* mu) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    Engine* e = &h->e;
+    GPE_RC(gpe::evolve(e, nt, mu));
+    return gpe::cuda_rc(cudaStreamSynchronize(e->st));
+}
+
+int gpe_gb_energy(gpe_gb_engine* h, double* t, double* ekin, double* eint, double* eext) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    if (!ekin || !eint || !eext) return GPE_ERR_ARGUMENT;
+    Engine* e = &h->e;
+    if (t) *t = e->t0 + e->dt * e->it;
+    return e->prec == GPE_PRECISION_FP32 ? gpe::energy<float>(e, ekin, eint, eext)
+                                         : gpe::energy<double>(e, ekin, eint, eext);
+}
+
+int gpe_gb_synchronize(gpe_gb_engine* h) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    return gpe::cuda_rc(cudaStreamSynchronize(h->e.st));
+}
+
+long long gpe_gb_kernel_launches(const gpe_gb_engine* h) { return h ? h->e.launches : -1; }
+
+void* gpe_gb_get_stream(const gpe_gb_engine* h) { return h ? (void*)h->e.st : nullptr; }
+
+int gpe_gb_use_graphs(gpe_gb_engine* h, int enable) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    h->e.use_graph = enable != 0;
+    return 0;
+}
+
+int gpe_gb_set_potential_slices(gpe_gb_engine* h, const double* fields, int nslices, int steps_per_slice) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    Engine* e = &h->e;
+    cudaStreamSynchronize(e->st);
+    cudaFree(e->vextra);
+    e->vextra = nullptr;
+    e->vslices = 0;
+    e->graph_dirty = true;
+    if (!fields) return 0;
+    if (nslices <= 0 || steps_per_slice <= 0) return GPE_ERR_ARGUMENT;
+    const size_t cnt = (size_t)nslices * e->n;
+    GPE_CK(cudaMalloc(&e->vextra, cnt * e->rsize()));
+    if (e->prec == GPE_PRECISION_FP64) {
+        GPE_CK(cudaMemcpy(e->vextra, fields, cnt * sizeof(double), cudaMemcpyHostToDevice));
+    } else {
+        std::vector<float> tmp(cnt);
+        for (size_t i = 0; i < cnt; i++) tmp[i] = (float)fields[i];
+        GPE_CK(cudaMemcpy(e->vextra, tmp.data(), cnt * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    e->vslices = nslices;
+    e->vsteps = steps_per_slice;
+    return 0;
+}
+
+const char* gpe_gb_error_string(int code) {
+    switch (code) {
+        case 0: return "success";
+        case GPE_ERR_TOO_MANY_PARAMS: return "too many user parameters";
+        case GPE_ERR_LATTICE: return "unsupported lattice: each side must be a power of two in [8, 512]";
+        case GPE_ERR_NO_ENGINE: return "engine not created";
+        case GPE_ERR_ARGUMENT: return "invalid argument";
+        case GPE_ERR_FUNCTIONAL: return "unknown interactions code";
+        case GPE_ERR_NOT_IMPLEMENTED: return "entry point not implemented by this engine";
+        default: break;
+    }
+    if (code > 0) return cudaGetErrorString((cudaError_t)code);
+    return "Unknown error!";
+}
+
+}  // extern "C"

@@ -1,0 +1,175 @@
+"""GPU engine against the CPU FP64 oracle, through the C ABI.
+
+FP64 plain form: <= 1e-12 relative L2 per step (both start each step from the
+same psi), drift after several steps, mu and energies.  FP32-mixed form:
+relative L2 <= 2e-5 per step and energies to 1e-5."""
+import numpy as np
+import pytest
+
+import oracle
+import libcugpe_gb300 as g
+from libcugpe_gb300 import configs
+
+pytestmark = pytest.mark.gpu
+
+TOL_FP64_STEP = 1e-12
+TOL_FP32_STEP = 2e-5
+
+CASES = {
+    # name: interactions, alpha, beta, qf, params, npart
+    "bec_ite": (-1, 0.0, 1.0, 0.0, [0.0625, 0.0625, 0.0625, 31.83], 1.0),
+    "bec_rte": (-1, 1.0, 0.0, 0.0, [0.0625, 0.05, 0.07, 31.83], 1.0),
+    "ufg_rte": (0, 1.0, 0.0, 0.0, [0.04, 0.04, 0.06, 0.0], 1000.0),
+    "ufg_rte_qf": (0, 1.0, 0.0, 0.1, [0.04, 0.04, 0.06, 0.0], 1000.0),
+    "ufg_ite_qf": (0, 0.0, 1.0, 0.1, [0.04, 0.04, 0.06, 0.0], 1000.0),
+    "bec_ite_qf": (-1, 0.0, 1.0, 0.2, [0.0625, 0.0625, 0.0625, 31.83], 1.0),
+    "bec_rte_qf": (-1, 1.0, 0.0, 0.3, [0.0625, 0.0625, 0.0625, 31.83], 1.0),
+    "becside_ite": (1, 0.0, 1.0, 0.0, [0.05, 0.05, 0.05, 2.0], 100.0),
+}
+SHAPES = [(16, 16, 16), (32, 16, 8), (8, 32, 16), (16, 8, 64), (128, 16, 8), (8, 256, 8), (512, 8, 16)]
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def make_pair(shape, case, precision=g.FP64, dt=0.05, seed=7):
+    inter, alpha, beta, qf, params, npart = CASES[case]
+    gamma = 1.0 if inter == -1 else 2.0
+    psi = configs.random_state(shape, seed=seed, npart=npart, gamma=gamma)
+    e = g.Engine(shape, inter, alpha, beta, dt, npart, precision=precision)
+    e.set_user_params(params)
+    o = oracle.Oracle(shape, inter, alpha, beta, dt, npart, threads=4)
+    o.set_user_params(params)
+    if qf:
+        e.set_quantum_friction_coeff(qf)
+        o.set_quantum_friction_coeff(qf)
+    e.set_psi(0.0, psi)
+    o.set_psi(0.0, psi)
+    return e, o, psi
+
+
+@pytest.mark.parametrize("case", list(CASES))
+@pytest.mark.parametrize("shape", SHAPES[:3])
+def test_fp64_per_step_parity(cuda_device, gpe_lib, case, shape):
+    e, o, psi = make_pair(shape, case)
+    beta = CASES[case][2]
+    for step in range(4):
+        mu_e = e.evolve_qf(1)
+        mu_o = o.evolve_qf(1)
+        _, pe = e.get_psi()
+        _, po = o.get_psi()
+        assert rel(pe, po) <= TOL_FP64_STEP, (step, rel(pe, po))
+        if beta != 0.0:
+            assert abs(mu_e - mu_o) <= 1e-10 * max(1.0, abs(mu_o))
+        e.set_psi(0.0, po)  # next step starts from the same psi again
+        o.set_psi(0.0, po)
+
+
+@pytest.mark.parametrize("shape", SHAPES[3:])
+@pytest.mark.parametrize("case", ["bec_ite", "ufg_rte_qf"])
+def test_fp64_parity_all_pencil_lengths(cuda_device, gpe_lib, case, shape):
+    e, o, _ = make_pair(shape, case)
+    e.evolve_qf(1)
+    o.evolve_qf(1)
+    assert rel(e.get_psi()[1], o.get_psi()[1]) <= TOL_FP64_STEP
+
+
+@pytest.mark.parametrize("case", ["bec_ite", "ufg_rte", "ufg_rte_qf", "ufg_ite_qf"])
+def test_fp64_multi_step_drift_and_energy(cuda_device, gpe_lib, case):
+    shape = (32, 16, 16)
+    e, o, _ = make_pair(shape, case)
+    for _ in range(3):
+        mu_e = e.evolve_qf(10)
+        mu_o = o.evolve_qf(10)
+    t_e, pe = e.get_psi()
+    t_o, po = o.get_psi()
+    assert t_e == pytest.approx(t_o, abs=1e-12)
+    assert rel(pe, po) <= 3e-11
+    if CASES[case][2] != 0.0:
+        assert abs(mu_e - mu_o) <= 1e-9 * max(1.0, abs(mu_o))
+    en_e, en_o = e.energy(), o.energy()
+    for a, b in zip(en_e[1:], en_o[1:]):
+        assert abs(a - b) <= 1e-10 * max(1.0, abs(b))
+    # the RTE energy call normalises psi in place on both sides
+    assert rel(e.get_psi()[1], o.get_psi()[1]) <= 3e-11
+    _, de = e.get_density()
+    _, do = o.get_density()
+    assert rel(de, do) <= 3e-11
+    assert e.get_norm() == pytest.approx(o.get_norm(), rel=1e-12)
+
+
+@pytest.mark.parametrize("case", ["bec_ite", "ufg_rte_qf", "ufg_ite_qf", "bec_rte"])
+def test_fp32_mixed_against_fp64_oracle(cuda_device, gpe_lib, case):
+    shape = (32, 16, 16)
+    e, o, _ = make_pair(shape, case, precision=g.FP32)
+    e.evolve_qf(1)
+    o.evolve_qf(1)
+    assert rel(e.get_psi()[1], o.get_psi()[1]) <= TOL_FP32_STEP
+    e.evolve_qf(20)
+    o.evolve_qf(20)
+    assert rel(e.get_psi()[1], o.get_psi()[1]) <= 20 * TOL_FP32_STEP
+    en_e, en_o = e.energy(), o.energy()
+    etot_e, etot_o = sum(en_e[1:]), sum(en_o[1:])
+    assert abs(etot_e - etot_o) <= 1e-5 * abs(etot_o)
+
+
+def test_graph_replay_is_bit_identical(cuda_device, gpe_lib):
+    shape = (16, 16, 32)
+    e1, _, psi = make_pair(shape, "ufg_ite_qf")
+    e2, _, _ = make_pair(shape, "ufg_ite_qf")
+    e2.use_graphs(False)
+    m1 = e1.evolve_qf(37)
+    m2 = e2.evolve_qf(37)
+    assert m1 == m2
+    assert np.array_equal(e1.get_psi()[1], e2.get_psi()[1])
+    n0 = e1.kernel_launches()
+    e1.evolve_qf(16)
+    assert e1.kernel_launches() - n0 >= 16 * 8
+
+
+def test_normalize_and_norm(cuda_device, gpe_lib):
+    shape = (16, 16, 16)
+    e, o, psi = make_pair(shape, "bec_rte")
+    e.set_psi(0.0, 3.0 * psi)
+    assert e.get_norm() == pytest.approx(9.0 * float(np.sum(np.abs(psi) ** 2)), rel=1e-13)
+    e.normalize_psi()
+    assert e.get_norm() == pytest.approx(1.0, rel=1e-13)
+
+
+def test_time_and_step_counter(cuda_device, gpe_lib):
+    shape = (16, 16, 16)
+    e, o, psi = make_pair(shape, "bec_ite", dt=0.02)
+    e.evolve_qf(5)
+    t, _ = e.get_psi()
+    assert t == pytest.approx(0.1)
+    e.set_time(1.0)
+    t, _ = e.get_psi()
+    assert t == pytest.approx(1.0)
+    e.set_psi(2.5, psi)
+    assert e.get_psi()[0] == 2.5
+
+
+def test_error_codes_on_gpu(cuda_device, gpe_lib):
+    e = g.Engine((16, 16, 16), -1, 0.0, 1.0, 0.1, 1.0)
+    with pytest.raises(g.GPEError) as ex:
+        e.set_user_params(np.zeros(33))
+    assert ex.value.code == g.ERR_TOO_MANY_PARAMS
+    with pytest.raises(g.GPEError) as ex:
+        g.Engine((16, 12, 16), -1, 0.0, 1.0, 0.1, 1.0)
+    assert ex.value.code == g.ERR_LATTICE
+
+
+def test_time_sliced_potential_matches_oracle(cuda_device, gpe_lib):
+    shape = (16, 16, 16)
+    e, o, _ = make_pair(shape, "bec_rte", dt=0.02)
+    rng = np.random.default_rng(11)
+    fields = 0.05 * rng.standard_normal((3,) + shape)
+    e.set_potential_slices(fields, 4)
+    o.set_vextra(fields, 4)
+    e.evolve_qf(10)
+    o.evolve_qf(10)
+    assert rel(e.get_psi()[1], o.get_psi()[1]) <= 1e-11
+    en_e, en_o = e.energy(), o.energy()
+    for a, b in zip(en_e[1:], en_o[1:]):
+        assert abs(a - b) <= 1e-10 * max(1.0, abs(b))

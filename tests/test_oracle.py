@@ -1,0 +1,151 @@
+"""The CPU FP64 oracle against an independent restatement, numpy's FFT,
+physics known answers, and the golden vectors recorded from the reference
+engine (tests/golden/)."""
+import glob
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from oracle.np_oracle import NpOracle
+from libcugpe_gb300 import configs
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("shape", [(8, 8, 8), (8, 16, 32), (32, 8, 16)])
+@pytest.mark.parametrize("sign", [-1, 1])
+def test_fft3d_matches_numpy(shape, sign):
+    rng = np.random.default_rng(3)
+    a = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    f = oracle.fft3d(a, sign, threads=2)
+    ref = np.fft.fftn(a) if sign < 0 else np.fft.ifftn(a) * a.size
+    assert rel(f, ref) < 1e-14
+
+
+CASES = [
+    # interactions, alpha, beta, qf, params, npart
+    (-1, 0.0, 1.0, 0.0, [0.0625, 0.0625, 0.0625, 31.83], 1.0),
+    (-1, 1.0, 0.0, 0.0, [0.0625, 0.05, 0.07, 31.83], 1.0),
+    (0, 1.0, 0.0, 0.0, [0.04, 0.04, 0.06, 0.0], 1000.0),
+    (0, 1.0, 0.0, 0.1, [0.04, 0.04, 0.06, 0.0], 1000.0),
+    (0, 0.0, 1.0, 0.1, [0.04, 0.04, 0.06, 0.0], 1000.0),
+    (-1, 0.0, 1.0, 0.2, [0.0625, 0.0625, 0.0625, 31.83], 1.0),
+]
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_matches_numpy_restatement(case):
+    inter, alpha, beta, qf, params, npart = case
+    shape = (16, 8, 32)
+    gamma = 1.0 if inter == -1 else 2.0
+    psi = configs.random_state(shape, seed=5, npart=npart, gamma=gamma)
+    o = oracle.Oracle(shape, inter, alpha, beta, 0.05, npart, threads=2)
+    o.set_user_params(params)
+    o.set_quantum_friction_coeff(qf)
+    o.set_psi(0.0, psi)
+    n = NpOracle(shape, inter, alpha, beta, 0.05, npart, params, qf)
+    n.psi = psi.copy()
+    mu1, mu2 = o.evolve_qf(4), n.evolve_qf(4)
+    _, p1 = o.get_psi()
+    assert rel(p1, n.psi) < 1e-13
+    if beta != 0:
+        assert abs(mu1 - mu2) < 1e-12 * max(1.0, abs(mu2))
+    _, ek, ei, ee = o.energy()
+    e2 = n.energy()
+    for a, b in zip((ek, ei, ee), e2):
+        assert abs(a - b) <= 1e-12 * max(1.0, abs(b))
+
+
+def test_oracle_thread_count_does_not_change_results():
+    shape = (16, 16, 16)
+    psi = configs.random_state(shape, seed=1, npart=1000.0, gamma=2.0)
+    out = []
+    for th in (1, 3):
+        o = oracle.Oracle(shape, 0, 1.0, 0.0, 0.05, 1000.0, threads=th)
+        o.set_user_params([0.04, 0.04, 0.06, 0.0])
+        o.set_quantum_friction_coeff(0.1)
+        o.set_psi(0.0, psi)
+        o.evolve_qf(3)
+        out.append(o.get_psi()[1])
+    assert np.array_equal(out[0], out[1])
+
+
+def test_ite_noninteracting_ground_state_energy():
+    # g = 0 isotropic trap: E/N -> 3/2 omega (lattice units), up to discretisation error
+    n, w = 32, 0.1
+    o = oracle.Oracle((n, n, n), -1, 0.0, 1.0, 0.2, 1.0, threads=4)
+    o.set_user_params([w, w, w, 0.0])
+    o.set_psi(0.0, configs.random_state((n, n, n), seed=2, phase=False))
+    o.normalize_psi()
+    mu = 0.0
+    for _ in range(20):
+        mu = o.evolve_qf(50)
+    _, ek, ei, ee = o.energy()
+    assert ei == 0.0
+    assert abs((ek + ee) - 1.5 * w) < 2e-3 * 1.5 * w
+    assert abs(mu - 1.5 * w) < 2e-3 * 1.5 * w
+
+
+def test_rte_conserves_norm_and_energy_without_friction():
+    shape = (16, 16, 16)
+    o = oracle.Oracle(shape, -1, 1.0, 0.0, 0.02, 1.0, threads=2)
+    o.set_user_params([0.1, 0.1, 0.1, 2.0])
+    o.set_psi(0.0, configs.random_state(shape, seed=4))
+    _, ek0, ei0, ee0 = o.energy()
+    n0 = o.get_norm()
+    o.evolve_qf(200)
+    assert abs(o.get_norm() - n0) < 1e-12
+    _, ek, ei, ee = o.energy()
+    assert abs((ek + ei + ee) - (ek0 + ei0 + ee0)) < 1e-4 * abs(ek0 + ei0 + ee0)
+
+
+def test_quantum_friction_cools():
+    shape = (16, 16, 16)
+    o = oracle.Oracle(shape, 0, 1.0, 0.0, 0.1, 100.0, threads=2)
+    o.set_user_params([0.1, 0.1, 0.12, 0.0])
+    o.set_quantum_friction_coeff(0.5)
+    o.set_psi(0.0, configs.random_state(shape, seed=6, npart=100.0, gamma=2.0))
+    es = []
+    for _ in range(5):
+        o.evolve_qf(20)
+        _, ek, ei, ee = o.energy()
+        es.append(ek + ei + ee)
+    assert all(b < a for a, b in zip(es, es[1:]))
+
+
+def golden_cases():
+    return sorted(glob.glob(os.path.join(GOLDEN, "*.json")))
+
+
+@pytest.mark.parametrize("path", golden_cases() or [None])
+def test_oracle_matches_reference_golden_vectors(path):
+    """Golden vectors are the reference engine's own outputs (tests/golden/make_golden.py)."""
+    if path is None:
+        pytest.skip("no golden vectors recorded")
+    meta = json.load(open(path))
+    data = np.load(path.replace(".json", ".npz"))
+    shape = tuple(meta["shape"])
+    o = oracle.Oracle(shape, meta["interactions"], meta["alpha"], meta["beta"], meta["dt"], meta["npart"], threads=2)
+    o.set_user_params(meta["params"])
+    if meta["qf"]:
+        o.set_quantum_friction_coeff(meta["qf"])
+    o.set_psi(0.0, data["psi0"])
+    if meta.get("normalize_first"):
+        o.normalize_psi()
+    for k, nsteps in enumerate(meta["steps"]):
+        mu = o.evolve_qf(nsteps)
+        _, p = o.get_psi()
+        ref = data[f"psi_{k}"]
+        assert rel(p, ref) < meta["tol_psi"], (k, rel(p, ref))
+        if meta["beta"] != 0:
+            assert abs(mu - meta["mu"][k]) < 1e-10 * max(1.0, abs(meta["mu"][k]))
+    t, ek, ei, ee = o.energy()
+    for a, b in zip((ek, ei, ee), meta["energy"]):
+        assert abs(a - b) < 1e-10 * max(1.0, abs(b))

@@ -1,0 +1,108 @@
+"""GPU engine against the reference libcugpe engine built for this GPU.
+
+The reference (dev/ engine, cuFFT Z2Z, FP64) is compiled by
+oracle/build_ref.py, one binary per lattice and functional, and driven by
+oracle/ref_runner.cpp through its own public API.  Both engines get the same
+seeded state; the FP64 drop-in must agree to <= 1e-12 relative L2 per step,
+and in energy, chemical potential and density after several steps.
+"""
+import numpy as np
+import pytest
+
+import libcugpe_gb300 as g
+from libcugpe_gb300 import configs
+from oracle import build_ref, ref_run
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    # shape, interactions, alpha, beta, dt, npart, params, qf
+    ((16, 16, 16), -1, 0.0, 1.0, 0.05, 1.0, [0.0625, 0.0625, 0.0625, 31.83], 0.0),
+    ((32, 16, 8), -1, 1.0, 0.0, 0.05, 1.0, [0.0625, 0.05, 0.07, 31.83], 0.0),
+    ((16, 16, 16), 0, 1.0, 0.0, 0.05, 1000.0, [0.04, 0.04, 0.06, 0.0], 0.1),
+    ((8, 32, 16), 0, 0.0, 1.0, 0.05, 1000.0, [0.04, 0.04, 0.06, 0.0], 0.1),
+    ((16, 16, 16), 0, 1.0, 0.0, 0.05, 1000.0, [0.04, 0.04, 0.06, 0.0], 0.0),
+    ((32, 32, 32), 0, 1.0, 0.0, 0.125, 1000.0, [0.04, 0.04, 0.06, 0.0], 0.1),
+]
+
+
+@pytest.fixture(scope="module")
+def reference(cuda_device):
+    if not ref_run.available():
+        pytest.skip("reference sources not available on this machine")
+    build_ref.build(sorted({(c[0][0], c[0][1], c[0][2], c[1]) for c in CASES} | {(64, 64, 64, -1)}))
+    return True
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def engine_for(shape, inter, alpha, beta, dt, npart, params, qf, psi):
+    e = g.Engine(shape, inter, alpha, beta, dt, npart)
+    e.set_user_params(params)
+    if qf:
+        e.set_quantum_friction_coeff(qf)
+    e.set_psi(0.0, psi)
+    return e
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c[0]}_i{c[1]}_b{c[3]}_qf{c[7]}")
+def test_per_step_parity_with_reference(reference, gpe_lib, case):
+    shape, inter, alpha, beta, dt, npart, params, qf = case
+    gamma = 1.0 if inter == -1 else 2.0
+    psi = configs.random_state(shape, seed=21, npart=npart, gamma=gamma)
+    # reference: 1 step, dump, 1 step, dump, ... ; ours restarts from the reference's psi each step
+    cmds = []
+    for _ in range(3):
+        cmds += ["S1", "D"]
+    out = ref_run.run(shape, inter, alpha, beta, dt, npart, params, psi, cmds, qf=qf)
+    prev = psi
+    for k, ref in enumerate(out["psi"]):
+        e = engine_for(shape, inter, alpha, beta, dt, npart, params, qf, prev)
+        mu = e.evolve_qf(1)
+        _, ours = e.get_psi()
+        assert rel(ours, ref) <= 1e-12, (k, rel(ours, ref))
+        if beta != 0.0:
+            assert abs(mu - out["mu"][k]) <= 1e-10 * max(1.0, abs(out["mu"][k]))
+        prev = ref
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c[0]}_i{c[1]}_b{c[3]}_qf{c[7]}")
+def test_energy_density_after_n_steps(reference, gpe_lib, case):
+    shape, inter, alpha, beta, dt, npart, params, qf = case
+    gamma = 1.0 if inter == -1 else 2.0
+    psi = configs.random_state(shape, seed=22, npart=npart, gamma=gamma)
+    n = 40
+    out = ref_run.run(shape, inter, alpha, beta, dt, npart, params, psi, ["E", f"S{n}", "E", "D"], qf=qf)
+    e = engine_for(shape, inter, alpha, beta, dt, npart, params, qf, psi)
+    e0 = e.energy()
+    mu = e.evolve_qf(n)
+    e1 = e.energy()
+    _, ours = e.get_psi()
+    ref = out["psi"][0]
+    assert rel(ours, ref) <= 1e-11, rel(ours, ref)
+    for ours_e, ref_e in ((e0, out["energy"][0]), (e1, out["energy"][1])):
+        assert ours_e[0] == pytest.approx(ref_e[0], abs=1e-12)
+        for a, b in zip(ours_e[1:], ref_e[1:]):
+            assert abs(a - b) <= 1e-10 * max(1.0, abs(b)), (a, b)
+    if beta != 0.0:
+        assert abs(mu - out["mu"][0]) <= 1e-9 * max(1.0, abs(out["mu"][0]))
+    dens_ours = gamma * np.abs(ours) ** 2
+    dens_ref = gamma * np.abs(ref) ** 2
+    assert rel(dens_ours, dens_ref) <= 2e-11
+
+
+def test_bec_64_ite_matches_reference(reference, gpe_lib):
+    """The 64^3 contact-BEC imaginary-time workload, 200 steps."""
+    w = configs.bec_ground_state_ite(n=64, steps=200)
+    out = ref_run.run(w.shape, -1, 0.0, 1.0, w.dt, w.npart, w.params, w.psi0, ["N", "S200", "E", "D"])
+    e = engine_for(w.shape, -1, 0.0, 1.0, w.dt, w.npart, w.params, 0.0, w.psi0)
+    e.normalize_psi()
+    mu = e.evolve_qf(200)
+    en = e.energy()
+    _, ours = e.get_psi()
+    assert rel(ours, out["psi"][0]) <= 1e-11
+    assert abs(mu - out["mu"][0]) <= 1e-9 * abs(out["mu"][0])
+    etot, etot_ref = sum(en[1:]), sum(out["energy"][0][1:])
+    assert abs(etot - etot_ref) <= 1e-11 * abs(etot_ref)
