@@ -277,6 +277,8 @@ def main():
     ap.add_argument("--block", type=int, default=100)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--ite-steps", type=int, default=200)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":
@@ -287,7 +289,7 @@ def main():
     import libcugpe_gb300 as g
     torch.cuda.set_device(local)
     w = workload(args.n)
-    psi = relaxed_state(w, 200)
+    psi = relaxed_state(w, args.ite_steps)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
 
     e32 = make_engine(w, psi, g.FP32)
@@ -326,7 +328,7 @@ def main():
         ref = reference_gpu(w, psi)
         if ref:
             extras["reference_gpu"] = ref
-        extras["cpu_baseline"] = cpu_baseline(w, psi, seconds=args.cpu_seconds if hasattr(args, "cpu_seconds") else 15.0)
+        extras["cpu_baseline"] = cpu_baseline(w, psi, seconds=args.cpu_seconds)
 
     if rank == 0:
         n = int(np.prod(w.shape))

@@ -128,7 +128,7 @@ struct AxisTables {
     void* ktab;   // C2<R>[N]  exp(c3 k^2 / Gamma^2) / N
     void* lqf;    // R[N]      (qf / Gamma) k^2 / N
     void* lek;    // R[N]      k^2 / (2 Gamma) / N
-    void* tw;     // C2<R>[N]  exp(-2 pi i p / N)
+    void* tw;     // C2<R>[tw_len]  stage-major twiddles (gpe_fft.cuh)
     void* vt;     // R[N]      0.5 i^2 w^2, i = index - N/2
 };
 
@@ -156,6 +156,7 @@ struct Engine {
 
     bool use_graph = true;
     bool graph_dirty = true;
+    bool lap_valid = false;  // lap holds the z-Laplacian term of the current psi
     cudaGraphExec_t gexec = nullptr;
     int gsteps = 0;
     int passes_per_step = 0;
@@ -194,6 +195,40 @@ static void step_coeff(const Engine* e, double* c3x, double* c3y) {
     *c3y = -a * bi / den;
 }
 
+template <int N> static void plan_of(int rad[3], int* L) {
+    rad[0] = Plan<N>::R0; rad[1] = Plan<N>::R1; rad[2] = Plan<N>::R2; *L = Plan<N>::L;
+}
+
+// Stage-major twiddles: stage s (Ns > 1) holds exp(-2 pi i r k / (Ns R)) at
+// r*Ns + k, stages packed in order (layout of tw_off / tw_len).
+template <typename R>
+static void stage_twiddles(int N, C2<R>* tw) {
+    int rad[3] = {1, 1, 1}, L = 1;
+    switch (N) {
+        case 8: plan_of<8>(rad, &L); break;
+        case 16: plan_of<16>(rad, &L); break;
+        case 32: plan_of<32>(rad, &L); break;
+        case 64: plan_of<64>(rad, &L); break;
+        case 128: plan_of<128>(rad, &L); break;
+        case 256: plan_of<256>(rad, &L); break;
+        default: plan_of<512>(rad, &L); break;
+    }
+    int off = 0, ns = rad[0];
+    tw[0].x = (R)1; tw[0].y = (R)0;
+    for (int s = 1; s < L; s++) {
+        const int R_ = rad[s];
+        for (int r = 0; r < R_; r++)
+            for (int k = 0; k < ns; k++) {
+                const long double ang = -2.0L * 3.14159265358979323846264338327950288L * (long double)(r * k) /
+                                        (long double)(ns * R_);
+                tw[off + r * ns + k].x = (R)(double)cosl(ang);
+                tw[off + r * ns + k].y = (R)(double)sinl(ang);
+            }
+        off += R_ * ns;
+        ns *= R_;
+    }
+}
+
 template <typename R>
 static int upload_tables(Engine* e) {
     double c3x, c3y;
@@ -202,7 +237,7 @@ static int upload_tables(Engine* e) {
     size_t off = 0;
     std::vector<unsigned char> host;
     size_t total = 0;
-    for (int a = 0; a < 3; a++) total += (size_t)e->n3[a] * (2 * sizeof(C2<R>) + 3 * sizeof(R)) + 256 * 5;
+    for (int a = 0; a < 3; a++) total += (size_t)e->n3[a] * (3 * sizeof(C2<R>) + 3 * sizeof(R)) + 256 * 5;
     host.assign(total, 0);
     if (!e->tabmem) GPE_CK(cudaMalloc(&e->tabmem, total));
     unsigned char* dbase = (unsigned char*)e->tabmem;
@@ -212,7 +247,7 @@ static int upload_tables(Engine* e) {
         std::vector<double> k;
         kgrid(k, N);
         const size_t okt = take(N * sizeof(C2<R>)), olq = take(N * sizeof(R)), ole = take(N * sizeof(R)),
-                     otw = take(N * sizeof(C2<R>)), ovt = take(N * sizeof(R));
+                     otw = take(2 * N * sizeof(C2<R>)), ovt = take(N * sizeof(R));
         C2<R>* kt = (C2<R>*)(host.data() + okt);
         R* lq = (R*)(host.data() + olq);
         R* le = (R*)(host.data() + ole);
@@ -229,13 +264,11 @@ static int upload_tables(Engine* e) {
             kt[i].y = (R)(ex * sin(zy) / (double)N);
             lq[i] = (R)((e->qf_raw / e->gamma) * (k[i] * k[i]) / (double)N);
             le[i] = (R)((k[i] * k[i]) / (2.0 * e->gamma) / (double)N);
-            const long double ang = -2.0L * 3.14159265358979323846264338327950288L * (long double)i / (long double)N;
-            tw[i].x = (R)(double)cosl(ang);
-            tw[i].y = (R)(double)sinl(ang);
             const double ii = (double)i - 1.0 * (N / 2);
             vt[i] = (R)(0.5 * ii * ii * w * w);  // dev/gpe_user_defined.h:500-510
         }
         e->ax[a].ktab = dbase + okt; e->ax[a].lqf = dbase + olq; e->ax[a].lek = dbase + ole;
+        stage_twiddles<R>(N, tw);
         e->ax[a].tw = dbase + otw; e->ax[a].vt = dbase + ovt;
     }
     GPE_CK(cudaMemcpyAsync(e->tabmem, host.data(), off, cudaMemcpyHostToDevice, e->st));
@@ -273,7 +306,7 @@ struct PassDesc {
 enum { B_NONE = 0, B_PSI = 1, B_PSI2 = 2 };
 
 // The reference step sequence (dev/gpe_engine.cu:1035-1106) as fused passes.
-static std::vector<PassDesc> schedule(const Engine* e) {
+static std::vector<PassDesc> schedule(const Engine* e, bool first) {
     std::vector<PassDesc> s;
     const bool ite = e->beta != 0.0;
     const bool qf = e->qf_raw != 0.0;
@@ -296,22 +329,25 @@ static std::vector<PassDesc> schedule(const Engine* e) {
                          B_PSI});
         }
     } else {
-        s.push_back({AX_Z, PRE_NONE, MID_LAP_STORE, POST_NONE, F_LAP | sin_, B_PSI, B_NONE});
+        // The z-Laplacian of psi comes from the last pass of the previous
+        // step (F_LAP_OUT); the first step after psi changed computes it.
+        if (first) s.push_back({AX_Z, PRE_NONE, MID_LAP_STORE, POST_NONE, F_LAP | sin_, B_PSI, B_NONE});
         s.push_back({AX_Y, PRE_NONE, MID_LAP_ACC, POST_NONE, F_LAP | sin_, B_PSI, B_NONE});
         s.push_back({AX_X, PRE_NONE, MID_QF_VSTEP1, POST_NONE, F_LAP | F_KIN | F_STORE | sin_, B_PSI, B_PSI2});
-        s.push_back({AX_Z, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI2, B_PSI2});
+        s.push_back({AX_Y, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI2, B_PSI2});
         if (!ite) {
-            s.push_back({AX_Y, PRE_NONE, MID_NONE, POST_PART12, F_KIN | F_STORE | F_QF | aux, B_PSI2, B_PSI});
+            s.push_back({AX_Z, PRE_NONE, MID_NONE, POST_PART12, F_KIN | F_STORE | F_QF | aux, B_PSI2, B_PSI});
             s.push_back({AX_X, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
-            s.push_back({AX_Z, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
-            s.push_back({AX_Y, PRE_NONE, MID_NONE, POST_VSTEP3, F_KIN | F_STORE | aux | F_FIN_STEP, B_PSI, B_PSI});
+            s.push_back({AX_Y, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
+            s.push_back({AX_Z, PRE_NONE, MID_NONE, POST_VSTEP3, F_KIN | F_STORE | aux | F_FIN_STEP | F_LAP_OUT, B_PSI,
+                         B_PSI});
         } else {
-            s.push_back({AX_Y, PRE_NONE, MID_NONE, POST_PART1, F_KIN | F_STORE | F_REDUCE | F_FIN_S2, B_PSI2, B_PSI2});
+            s.push_back({AX_Z, PRE_NONE, MID_NONE, POST_PART1, F_KIN | F_STORE | F_REDUCE | F_FIN_S2, B_PSI2, B_PSI2});
             s.push_back({AX_X, PRE_PART2, MID_NONE, POST_NONE,
                          F_KIN | F_STORE | F_SCALE_IN | F_SCALE_PSI2 | F_QF | aux, B_PSI, B_PSI});
-            s.push_back({AX_Z, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
-            s.push_back({AX_Y, PRE_NONE, MID_NONE, POST_VSTEP3, F_KIN | F_STORE | aux | F_REDUCE | F_FIN_STEP, B_PSI,
-                         B_PSI});
+            s.push_back({AX_Y, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
+            s.push_back({AX_Z, PRE_NONE, MID_NONE, POST_VSTEP3,
+                         F_KIN | F_STORE | aux | F_REDUCE | F_FIN_STEP | F_LAP_OUT, B_PSI, B_PSI});
         }
     }
     return s;
@@ -419,14 +455,20 @@ static const int kGraphSteps = 16;
 
 static int evolve(Engine* e, int nt, double* mu) {
     if (nt <= 0) return 0;
-    const std::vector<PassDesc> s = schedule(e);
+    const bool qf = e->qf_raw != 0.0;
+    const std::vector<PassDesc> s = schedule(e, false);
     e->passes_per_step = (int)s.size();
     int done = 0;
+    if (qf && !e->lap_valid) {
+        // psi changed since the last step: this step also computes the z-Laplacian
+        GPE_RC(run_steps(e, schedule(e, true), 1));
+        done = 1;
+    }
     if (e->use_graph) {
-        // first steps run directly: this also configures every kernel outside capture
-        if (e->graph_dirty || !e->gexec) {
+        // one step runs directly first: this also configures every kernel outside capture
+        if ((e->graph_dirty || !e->gexec) && nt - done >= 1) {
             GPE_RC(run_steps(e, s, 1));
-            done = 1;
+            done += 1;
             if (nt - done >= 2) GPE_RC(build_graph(e, s, nt - done < kGraphSteps ? nt - done : kGraphSteps));
         }
         while (e->gexec && nt - done >= e->gsteps) {
@@ -436,8 +478,10 @@ static int evolve(Engine* e, int nt, double* mu) {
         }
     }
     GPE_RC(run_steps(e, s, nt - done));
+    e->lap_valid = qf;
     if (e->beta != 0.0) {
         GPE_RC(e->prec == GPE_PRECISION_FP32 ? finish_ite<float>(e) : finish_ite<double>(e));
+        e->lap_valid = false;  // psi was rescaled
         if (mu) {
             double m = 0.0;
             GPE_CK(cudaMemcpyAsync(&m, &e->dyn->mu, sizeof(double), cudaMemcpyDeviceToHost, e->st));
@@ -458,6 +502,7 @@ static int norm_to_slot(Engine* e, int slot) {
 
 template <typename R>
 static int normalize_psi(Engine* e) {
+    e->lap_valid = false;
     GPE_RC(norm_to_slot<R>(e, 12));
     int b, t;
     util_grid(e->n, &b, &t);
@@ -497,7 +542,7 @@ static int energy(Engine* e, double* ekin, double* eint, double* eext) {
 static size_t max_grid(const Engine* e) {
     size_t g = kRedBlocks;
     for (int a = 0; a < 3; a++) {
-        const size_t p = pass_grid(e->n3[a], pencils_of(e, a));
+        const size_t p = pass_grid_bound(pencils_of(e, a));
         if (p > g) g = p;
     }
     return g;
@@ -611,6 +656,7 @@ int gpe_gb_set_quantum_friction_coeff(gpe_gb_engine* h, double q) {
     if (!h) return GPE_ERR_NO_ENGINE;
     Engine* e = &h->e;
     e->qf_raw = q;
+    e->lap_valid = false;
     if (q != 0.0) {
         if (!e->lap) GPE_CK(cudaMalloc(&e->lap, e->csize() * e->n));
         if (!e->Vqf) GPE_CK(cudaMalloc(&e->Vqf, e->rsize() * e->n));
@@ -641,6 +687,7 @@ static int set_psi_from(Engine* e, double t, const void* src, cudaMemcpyKind kin
     }
     e->t0 = t;
     e->it = 0;
+    e->lap_valid = false;
     GPE_RC(gpe::set_state(e, 0, 1.0));
     return gpe::cuda_rc(cudaStreamSynchronize(e->st));
 }

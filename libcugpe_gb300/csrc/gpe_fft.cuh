@@ -115,17 +115,46 @@ template <int N, int S> __host__ __device__ constexpr int plan_ns() {
     return S == 0 ? 1 : S == 1 ? Plan<N>::R0 : Plan<N>::R0 * Plan<N>::R1;
 }
 
-// One Stockham stage.  `sb` is this pencil's row in shared memory (point p at
-// sb[p * SSTR]); `tw` holds exp(-2 pi i p / N), p < N.  The last stage keeps
-// its result in registers; the others exchange through `sb`.
-template <typename R, int N, int S, bool INV, int SSTR>
-__device__ __forceinline__ void stage(C2<R> (&v)[Plan<N>::E], C2<R>* sb, int t, const C2<R>* __restrict__ tw) {
+// Stage-major twiddle table: stage S (Ns > 1) owns RAD*Ns entries at
+// tw_off<N, S>(), entry r*Ns + k = exp(-2 pi i r k / (Ns RAD)), so the lanes of
+// a stage (consecutive k) read consecutive entries.
+template <int N, int S> __host__ __device__ constexpr int tw_off() {
+    return (S <= 1) ? 0 : plan_rad<N, 1>() * plan_ns<N, 1>();
+}
+template <int N> __host__ __device__ constexpr int tw_len() {
+    return (Plan<N>::L == 1) ? 1
+         : (Plan<N>::L == 2) ? plan_rad<N, 1>() * plan_ns<N, 1>()
+         : plan_rad<N, 1>() * plan_ns<N, 1>() + plan_rad<N, 2>() * plan_ns<N, 2>();
+}
+
+// Exchange layout: point p of a pencil sits at padp(p) * SSTR, one padding
+// slot per 16 points, so the power-of-two strides of the Stockham stores
+// spread over the shared-memory banks.
+__host__ __device__ __forceinline__ constexpr int padp(int p) { return p + (p >> 4); }
+template <int N> __host__ __device__ constexpr int padded_len() { return N + N / 16 + (N < 16 ? 1 : 0); }
+
+// Barrier over the G threads that exchange one group of pencils: a warp
+// barrier when the group lies inside one warp, else a named barrier.
+template <int G> __device__ __forceinline__ void group_sync(int bar) {
+    if constexpr (G <= 32) {
+        __syncwarp();
+    } else {
+        asm volatile("bar.sync %0, %1;" ::"r"(bar), "n"(G) : "memory");
+    }
+}
+
+// One Stockham stage, computed in place in registers.  `sb` addresses this
+// thread's pencil in shared memory (point p at sb[padp(p) * SSTR]); `tw` is
+// the stage-major twiddle table (tw_off / tw_len).  The last stage keeps its
+// result in registers; the others exchange through `sb`.
+template <typename R, int N, int S, bool INV, int SSTR, int G>
+__device__ __forceinline__ void stage(C2<R> (&v)[Plan<N>::E], C2<R>* sb, int t, const C2<R>* tw, int bar) {
     constexpr int E = Plan<N>::E, T = N / E, L = Plan<N>::L;
     constexpr int RAD = plan_rad<N, S>();
     constexpr int NS = plan_ns<N, S>();
     constexpr int MB = E / RAD;
     constexpr bool LAST = (S == L - 1);
-    C2<R> o[E];
+    if constexpr (!LAST) group_sync<G>(bar);  // earlier readers of sb are done
 #pragma unroll
     for (int m = 0; m < MB; m++) {
         const int j = t + m * T;
@@ -136,40 +165,34 @@ __device__ __forceinline__ void stage(C2<R> (&v)[Plan<N>::E], C2<R>* sb, int t, 
         if constexpr (NS > 1) {
 #pragma unroll
             for (int r = 1; r < RAD; r++) {
-                C2<R> w = tw[r * k * (N / (NS * RAD))];
+                C2<R> w = tw[tw_off<N, S>() + r * NS + k];
                 if constexpr (INV) w.y = -w.y;
                 u[r] = cmul(u[r], w);
             }
         }
         dft<R, RAD, INV>(u);
+        if constexpr (LAST) {
 #pragma unroll
-        for (int r = 0; r < RAD; r++) o[m + r * MB] = u[r];
-    }
-    if constexpr (LAST) {
-#pragma unroll
-        for (int q = 0; q < E; q++) v[q] = o[q];
-    } else {
-        __syncthreads();  // earlier readers of sb are done
-#pragma unroll
-        for (int m = 0; m < MB; m++) {
-            const int j = t + m * T;
-            const int k = j & (NS - 1);
+            for (int r = 0; r < RAD; r++) v[m + r * MB] = u[r];
+        } else {
             const int base = (j - k) * RAD + k;
 #pragma unroll
-            for (int r = 0; r < RAD; r++) sb[(base + r * NS) * SSTR] = o[m + r * MB];
+            for (int r = 0; r < RAD; r++) sb[padp(base + r * NS) * SSTR] = u[r];
         }
-        __syncthreads();
+    }
+    if constexpr (!LAST) {
+        group_sync<G>(bar);
 #pragma unroll
-        for (int q = 0; q < E; q++) v[q] = sb[(t + T * q) * SSTR];
+        for (int q = 0; q < E; q++) v[q] = sb[padp(t + T * q) * SSTR];
     }
 }
 
 // Unnormalised transform, forward (exp(-2 pi i jk/N)) or inverse (exp(+...)).
-template <typename R, int N, bool INV, int SSTR>
-__device__ __forceinline__ void fft(C2<R> (&v)[Plan<N>::E], C2<R>* sb, int t, const C2<R>* __restrict__ tw) {
-    stage<R, N, 0, INV, SSTR>(v, sb, t, tw);
-    if constexpr (Plan<N>::L > 1) stage<R, N, 1, INV, SSTR>(v, sb, t, tw);
-    if constexpr (Plan<N>::L > 2) stage<R, N, 2, INV, SSTR>(v, sb, t, tw);
+template <typename R, int N, bool INV, int SSTR, int G>
+__device__ __forceinline__ void fft(C2<R> (&v)[Plan<N>::E], C2<R>* sb, int t, const C2<R>* tw, int bar) {
+    stage<R, N, 0, INV, SSTR, G>(v, sb, t, tw, bar);
+    if constexpr (Plan<N>::L > 1) stage<R, N, 1, INV, SSTR, G>(v, sb, t, tw, bar);
+    if constexpr (Plan<N>::L > 2) stage<R, N, 2, INV, SSTR, G>(v, sb, t, tw, bar);
 }
 
 }  // namespace gpe

@@ -1,5 +1,5 @@
 // Launch dispatch for the fused pencil pass: maps a run-time pencil length
-// and axis to the compiled kernel, picks pencils per CTA and the dynamic
+// and axis to the compiled kernel, picks the CTA shape and the dynamic
 // shared memory.  The kernels are instantiated in one generated translation
 // unit per (precision, pencil length) so they compile in parallel.
 #pragma once
@@ -8,39 +8,39 @@
 
 namespace gpe {
 
-// Threads per CTA for the fused pass.
-constexpr int kPassThreads = 128;
-
-template <int N> constexpr int wide_w() { return kPassThreads / (N / Plan<N>::E); }
-template <int N> constexpr int narrow_w() {
-    return (32 / (N / Plan<N>::E)) > 0 ? (32 / (N / Plan<N>::E)) : 1;
+// Threads per CTA: 128, or one pencil group when a group is larger; a
+// narrow variant (one group or one warp) serves lattices with few pencils.
+template <typename R, int N, int AX> constexpr int wide_nt() {
+    constexpr int g = PassGeom<R, N, AX, 128>::G;
+    return g > 128 ? g : 128;
+}
+template <typename R, int N, int AX> constexpr int narrow_nt() {
+    constexpr int g = (AX == AX_Z) ? 32 : (N / Plan<N>::E) * PassGeom<R, N, AX, 128>::CW;
+    return g < 32 ? 32 : g;
 }
 
-template <typename R, int N, int AX, int W>
-size_t pass_smem() {
-    return (AX == AX_Z) ? (size_t)W * (N + 1) * sizeof(C2<R>) : (size_t)W * N * sizeof(C2<R>);
-}
-
-template <typename R, int N, int AX, int W>
+template <typename R, int N, int AX, int NT>
 cudaError_t launch_one(const PassArgs<R>& a, size_t pencils, cudaStream_t st) {
-    const size_t smem = pass_smem<R, N, AX, W>();
-    static bool configured = false;  // per instantiation; attribute is per-device-context
+    using Geo = PassGeom<R, N, AX, NT>;
+    static bool configured = false;  // per instantiation, single device
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(pass_kernel<R, N, AX, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(pass_kernel<R, N, AX, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)Geo::SMEM_MAX);
         if (e != cudaSuccess) return e;
         configured = true;
     }
-    const unsigned grid = (unsigned)(pencils / W);
-    pass_kernel<R, N, AX, W><<<grid, W * (N / Plan<N>::E), smem, st>>>(a);
+    const unsigned grid = (unsigned)(pencils / Geo::W);
+    const size_t smem = Geo::SMEM_BASE + slot_bytes<R>(staged_ops(a.mid, a.post, a.flags), Geo::E * NT);
+    pass_kernel<R, N, AX, NT><<<grid, NT, smem, st>>>(a);
     return cudaGetLastError();
 }
 
 template <typename R, int N, int AX>
 cudaError_t launch_ax(const PassArgs<R>& a, size_t pencils, cudaStream_t st, unsigned* grid_out) {
-    constexpr int WW = wide_w<N>(), WN = narrow_w<N>();
-    if (pencils % WW == 0) { *grid_out = (unsigned)(pencils / WW); return launch_one<R, N, AX, WW>(a, pencils, st); }
-    if (pencils % WN == 0) { *grid_out = (unsigned)(pencils / WN); return launch_one<R, N, AX, WN>(a, pencils, st); }
+    constexpr int NW = wide_nt<R, N, AX>(), NN = narrow_nt<R, N, AX>();
+    constexpr int WW = PassGeom<R, N, AX, NW>::W, WN = PassGeom<R, N, AX, NN>::W;
+    if (pencils % WW == 0) { *grid_out = (unsigned)(pencils / WW); return launch_one<R, N, AX, NW>(a, pencils, st); }
+    if (pencils % WN == 0) { *grid_out = (unsigned)(pencils / WN); return launch_one<R, N, AX, NN>(a, pencils, st); }
     return cudaErrorInvalidValue;
 }
 
@@ -58,22 +58,8 @@ cudaError_t launch_n(const PassArgs<R>& a, int axis, size_t pencils, cudaStream_
 }
 #endif
 
-// Number of CTAs a pass over `pencils` pencils of length N would use.
-inline unsigned pass_grid(int N, size_t pencils) {
-    int T = 1;
-    switch (N) {
-        case 8: T = 8 / Plan<8>::E; break;
-        case 16: T = 16 / Plan<16>::E; break;
-        case 32: T = 32 / Plan<32>::E; break;
-        case 64: T = 64 / Plan<64>::E; break;
-        case 128: T = 128 / Plan<128>::E; break;
-        case 256: T = 256 / Plan<256>::E; break;
-        default: T = 512 / Plan<512>::E; break;
-    }
-    const int ww = kPassThreads / T, wn = (32 / T) > 0 ? 32 / T : 1;
-    if (pencils % ww == 0) return (unsigned)(pencils / ww);
-    return (unsigned)(pencils / wn);
-}
+// Upper bound on the CTAs of a pass over `pencils` pencils (sizes the partials buffer).
+inline size_t pass_grid_bound(size_t pencils) { return pencils; }
 
 template <typename R>
 cudaError_t launch_pass(const PassArgs<R>& a, int N, int axis, size_t pencils, cudaStream_t st) {
@@ -93,6 +79,6 @@ cudaError_t launch_pass(const PassArgs<R>& a, int N, int axis, size_t pencils, c
 }  // namespace gpe
 
 // One translation unit per (precision, pencil length) instantiates
-// launch_n<R, N>; launch_pass<R> (gpe_engine.cu) switches over them.
+// launch_n<R, N>; launch_pass<R> switches over them.
 #define GPE_INSTANTIATE_N(R, N) \
     template cudaError_t gpe::launch_n<R, N>(const gpe::PassArgs<R>&, int, size_t, cudaStream_t, unsigned*);

@@ -58,6 +58,7 @@ enum : uint32_t {  // flags
     F_EKIN = 1u << 10,      // forward transform only, accumulate sum w_k |X_k|^2
     F_FIN_RED = 1u << 11,   // last CTA: store the NRED sums in dyn->red[red_slot..]
     F_VEXTRA = 1u << 12,    // time-sliced additive potential table
+    F_LAP_OUT = 1u << 13,   // after the store: lap = D_a(result) (Laplacian of the new psi)
 };
 
 // Scalars that change while a step runs; they live in device memory so one
@@ -102,13 +103,13 @@ struct PassArgs {
     Phys<R> ph;
 };
 
-template <typename R> __device__ __forceinline__ R vext_at(const PassArgs<R>& a, size_t idx, int ix, int iy, int iz,
+template <typename R> __device__ __forceinline__ R vext_at(const PassArgs<R>& a, uint32_t idx, int ix, int iy, int iz,
                                                           unsigned it) {
     R v = (__ldg(a.vx + ix) + __ldg(a.vy + iy)) + __ldg(a.vz + iz);
     if (a.flags & F_VEXTRA) {
         int s = (int)(it / (unsigned)a.vsteps);
         if (s >= a.vslices) s = a.vslices - 1;
-        v += a.vextra[(size_t)s << (a.lx + a.ly + a.lz) | idx];
+        v += a.vextra[((size_t)s << (a.lx + a.ly + a.lz)) | idx];
     }
     return v;
 }
@@ -175,59 +176,196 @@ __device__ void finalize(const PassArgs<R>& a, double (*sred)[NRED]) {
     }
 }
 
-template <typename R, int N, int AX, int W>
-__global__ void __launch_bounds__(W * (N / Plan<N>::E))
+// Operands that the MID/POST ops read after the transforms.  They are
+// prefetched into shared memory with cp.async when the CTA starts, so their
+// latency overlaps the transforms instead of stalling the epilogue.
+enum : uint32_t {
+    OP_PSI = 1u << 0,   // C2 psi            (corrector)
+    OP_LAP = 1u << 1,   // C2 lap            (Laplacian accumulate / V_qf)
+    OP_AUXC = 1u << 2,  // C2 exp(c3 V')     (Vstep3, FP64)
+    OP_COPY = 1u << 3,  // C2 loaded value   (kept for V_qf, from registers)
+    OP_V = 1u << 4,     // R  V              (corrector)
+    OP_AUXR = 1u << 5,  // R  V'             (Vstep3, FP32)
+    OP_VQF = 1u << 6,   // R  V_qf           (corrector with friction)
+};
+
+__host__ __device__ inline uint32_t staged_ops(int mid, int post, uint32_t flags) {
+    uint32_t m = 0;
+    if (mid == MID_LAP_ACC) m |= OP_LAP;
+    if (mid == MID_QF_VSTEP1) m |= OP_LAP | OP_COPY;
+    if (post == POST_VSTEP2 || post == POST_PART12) m |= OP_PSI | OP_V;
+    if (post == POST_PART12 && (flags & F_QF)) m |= OP_VQF;
+    if (post == POST_PART1) m |= OP_V;
+    if (post == POST_VSTEP3) m |= (flags & F_AUX_CPLX) ? OP_AUXC : OP_AUXR;
+    return m;
+}
+
+// Slots: A (C2) = psi | lap | aux-complex, B (C2) = copy, C (R) = V | aux-real,
+// D (R) = V_qf; each E*NT elements, element (q, thread) at q*NT + thread.
+template <typename R>
+__host__ __device__ inline size_t slot_bytes(uint32_t m, int per_cta) {
+    size_t b = 0;
+    if (m & (OP_PSI | OP_LAP | OP_AUXC)) b += (size_t)per_cta * sizeof(C2<R>);
+    if (m & OP_COPY) b += (size_t)per_cta * sizeof(C2<R>);
+    if (m & (OP_V | OP_AUXR)) b += (size_t)per_cta * sizeof(R);
+    if (m & OP_VQF) b += (size_t)per_cta * sizeof(R);
+    return b;
+}
+
+__device__ __forceinline__ void cp_async(void* dst, const void* src, int bytes) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+    if (bytes == 16) asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(src) : "memory");
+    else if (bytes == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(src) : "memory");
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// Geometry of one pass kernel instantiation.
+//  z pencils: a warp holds 32/T whole pencils, t fastest (coalesced rows).
+//  y/x pencils: a group of G = T*CW threads holds CW adjacent columns, column
+//  fastest, so every warp-wide access covers >= 32 contiguous bytes per row.
+template <typename R, int N, int AX, int NT>
+struct PassGeom {
+    static constexpr int E = Plan<N>::E;
+    static constexpr int T = N / E;
+    static constexpr int CWMIN = (sizeof(C2<R>) == 8) ? 4 : 2;
+    static constexpr int CW = (AX == AX_Z) ? (32 / T) : ((32 / T) > CWMIN ? (32 / T) : CWMIN);
+    static constexpr int G = (AX == AX_Z) ? 32 : T * CW;
+    static constexpr int W = NT / T;  // pencils per CTA
+    static constexpr int ROW = padded_len<N>();
+    static constexpr int TW = tw_len<N>();
+    static constexpr size_t TAB_BYTES = (((size_t)(TW + N) * sizeof(C2<R>) + N * sizeof(R)) + 15) & ~(size_t)15;
+    static constexpr size_t EXCH_BYTES = (size_t)W * ROW * sizeof(C2<R>);
+    static constexpr size_t SMEM_BASE = TAB_BYTES + EXCH_BYTES;
+    static constexpr size_t SMEM_MAX = SMEM_BASE + 2 * (size_t)E * NT * (sizeof(C2<R>) + sizeof(R));
+    static constexpr int MINB = (sizeof(R) == 4 ? 512 : 256) / NT;
+    static_assert(NT % G == 0 && NT % 32 == 0, "threads per CTA must hold whole groups");
+};
+
+template <typename R, int N, int AX, int NT>
+__global__ void __launch_bounds__(NT, PassGeom<R, N, AX, NT>::MINB)
 pass_kernel(const PassArgs<R> a) {
-    constexpr int E = Plan<N>::E, T = N / E, NT = W * T;
-    constexpr int SSTR = (AX == AX_Z) ? 1 : W;
+    using Geo = PassGeom<R, N, AX, NT>;
+    constexpr int E = Geo::E, T = Geo::T, CW = Geo::CW, G = Geo::G, W = Geo::W, ROW = Geo::ROW;
+    constexpr int SSTR = (AX == AX_Z) ? 1 : CW;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    C2<R>* smem = reinterpret_cast<C2<R>*>(smem_raw);
-    __shared__ double sred[(NT + 31) / 32][NRED];
+    C2<R>* stw = reinterpret_cast<C2<R>*>(smem_raw);
+    C2<R>* skt = stw + Geo::TW;
+    R* slt = reinterpret_cast<R*>(skt + N);
+    C2<R>* sx = reinterpret_cast<C2<R>*>(smem_raw + Geo::TAB_BYTES);
+    __shared__ double sred[NT / 32][NRED];
     __shared__ bool last_cta;
 
     const int tid = threadIdx.x;
-    int pl, t;
-    if constexpr (AX == AX_Z) { t = tid % T; pl = tid / T; }
-    else { pl = tid % W; t = tid / W; }
-    C2<R>* sb = (AX == AX_Z) ? smem + pl * (N + 1) : smem + pl;
+    for (int i = tid; i < Geo::TW; i += NT) stw[i] = a.tw[i];
+    for (int i = tid; i < N; i += NT) {
+        skt[i] = a.ktab[i];
+        slt[i] = a.ltab[i];
+    }
+    // staged operand slots (see staged_ops)
+    const uint32_t ops = staged_ops(a.mid, a.post, a.flags);
+    unsigned char* sop = smem_raw + Geo::SMEM_BASE;
+    C2<R>* slotA = reinterpret_cast<C2<R>*>(sop);
+    if (ops & (OP_PSI | OP_LAP | OP_AUXC)) sop += (size_t)E * NT * sizeof(C2<R>);
+    C2<R>* slotB = reinterpret_cast<C2<R>*>(sop);
+    if (ops & OP_COPY) sop += (size_t)E * NT * sizeof(C2<R>);
+    R* slotC = reinterpret_cast<R*>(sop);
+    if (ops & (OP_V | OP_AUXR)) sop += (size_t)E * NT * sizeof(R);
+    R* slotD = reinterpret_cast<R*>(sop);
 
-    const size_t gp = (size_t)blockIdx.x * W + pl;  // pencil id
-    const int lx = a.lx, ly = a.ly, lz = a.lz;
-    size_t base, estr;
-    if constexpr (AX == AX_Z) { base = gp << lz; estr = 1; }
+    int pl, t, bar;
+    C2<R>* sb;
+    if constexpr (AX == AX_Z) {
+        const int w = tid >> 5, lane = tid & 31;
+        t = lane % T;
+        pl = w * CW + lane / T;
+        sb = sx + pl * ROW;
+        bar = 0;
+    } else {
+        const int gi = tid / G, loc = tid % G;
+        const int c = loc % CW;
+        t = loc / CW;
+        pl = gi * CW + c;
+        sb = sx + gi * (ROW * CW) + c;
+        bar = 1 + gi;
+    }
+
+    // 32-bit point indices: the largest lattice (512^3) has 2^27 points
+    const uint32_t gp = blockIdx.x * (uint32_t)W + pl;  // pencil id
+    const int ly = a.ly, lz = a.lz;
+    uint32_t base, lstr;  // first point of the pencil, log2 of the point stride
+    if constexpr (AX == AX_Z) { base = gp << lz; lstr = 0; }
     else if constexpr (AX == AX_Y) {
-        const size_t ix = gp >> lz, iz = gp & ((1u << lz) - 1);
-        base = ((ix << ly) << lz) + iz; estr = (size_t)1 << lz;
-    } else { base = gp; estr = (size_t)1 << (ly + lz); }
-    (void)lx;
+        const uint32_t ix = gp >> lz, iz = gp & ((1u << lz) - 1);
+        base = ((ix << ly) << lz) + iz; lstr = lz;
+    } else { base = gp; lstr = ly + lz; }
+    const uint32_t tbase = base + ((uint32_t)t << lstr);
+    auto at = [&](int q) -> uint32_t { return tbase + ((uint32_t)(T * q) << lstr); };
+    auto decode = [&](uint32_t idx, int& ix, int& iy, int& iz) {
+        ix = (int)(idx >> (ly + lz));
+        iy = (int)((idx >> lz) & ((1u << ly) - 1));
+        iz = (int)(idx & ((1u << lz) - 1));
+    };
 
     const DynState* dyn = a.dyn;
     const unsigned it = dyn->it;
     const R s_prev = (R)dyn->s_prev;
+    const bool scale_in = (a.flags & F_SCALE_IN) != 0;
 
     C2<R> x[E];
 #pragma unroll
-    for (int q = 0; q < E; q++) x[q] = ldc(a.in + base + (size_t)(t + T * q) * estr);
+    for (int q = 0; q < E; q++) x[q] = ldc(a.in + at(q));
+    if (ops) {
+        const void* srcA = (ops & OP_PSI) ? (const void*)a.psi : (ops & OP_LAP) ? (const void*)a.lap : a.aux;
+        const void* srcC = (ops & OP_V) ? (const void*)a.V : a.aux;
+#pragma unroll
+        for (int q = 0; q < E; q++) {
+            const uint32_t idx = at(q);
+            if (ops & (OP_PSI | OP_LAP | OP_AUXC))
+                cp_async(slotA + q * NT + tid, reinterpret_cast<const C2<R>*>(srcA) + idx, sizeof(C2<R>));
+            if (ops & (OP_V | OP_AUXR)) cp_async(slotC + q * NT + tid, reinterpret_cast<const R*>(srcC) + idx, sizeof(R));
+            if (ops & OP_VQF) cp_async(slotD + q * NT + tid, a.Vqf + idx, sizeof(R));
+        }
+        cp_async_commit();
+    }
+#pragma unroll
+    for (int q = 0; q < E; q++)
+        if (scale_in) x[q] = cscale(x[q], s_prev);
+    __syncthreads();  // tables staged
 
     double acc[NRED] = {0.0, 0.0, 0.0};
 
-    // ---------------------------------------------------------------- PRE
-    if (a.flags & F_SCALE_IN) {
+    // The pointwise ops below run in rolled loops over this thread's own
+    // cells of the exchange buffer (positions t + T*q, which only this thread
+    // reads between transforms; every exchange starts with a group barrier),
+    // so their transcendental-heavy bodies appear once in the instruction
+    // stream instead of E times.
+    auto own = [&](int q) -> C2<R>& { return sb[padp(t + T * q) * SSTR]; };
+    auto to_cells = [&]() {
 #pragma unroll
-        for (int q = 0; q < E; q++) x[q] = cscale(x[q], s_prev);
-    }
+        for (int q = 0; q < E; q++) own(q) = x[q];
+    };
+    auto from_cells = [&]() {
+#pragma unroll
+        for (int q = 0; q < E; q++) x[q] = own(q);
+    };
+
+    // ---------------------------------------------------------------- PRE
     if (a.pre != PRE_NONE) {
         const R s2 = (R)dyn->s2;
-#pragma unroll
+        to_cells();
+#pragma unroll 1
         for (int q = 0; q < E; q++) {
-            const size_t idx = base + (size_t)(t + T * q) * estr;
-            const int ix = (int)(idx >> (ly + lz)), iy = (int)((idx >> lz) & ((1u << ly) - 1)),
-                      iz = (int)(idx & ((1u << lz) - 1));
+            const uint32_t idx = at(q);
+            int ix, iy, iz;
+            decode(idx, ix, iy, iz);
+            C2<R> v = own(q);
             if (a.pre == PRE_VSTEP1) {
-                const R rho = density(a.ph, x[q]);
+                const R rho = density(a.ph, v);
                 const R V = vext_at(a, idx, ix, iy, iz, it) + dEDFdn(a.ph, rho);
                 a.V[idx] = V;
-                x[q] = cmul(x[q], phase(a.ph, V));
+                v = cmul(v, phase(a.ph, V));
             } else if (a.pre == PRE_PART2) {
                 C2<R> p2 = a.psi2[idx];
                 if (a.flags & F_SCALE_PSI2) p2 = cscale(p2, s2);
@@ -238,94 +376,112 @@ pass_kernel(const PassArgs<R> a) {
                 const C2<R> e = phase(a.ph, lv);
                 if (a.flags & F_AUX_CPLX) reinterpret_cast<C2<R>*>(a.aux)[idx] = e;
                 else reinterpret_cast<R*>(a.aux)[idx] = lv;
-                x[q] = cmul(x[q], e);
+                v = cmul(v, e);
             } else if (a.pre == PRE_ENERGY) {
-                const C2<double> pd = make_double2((double)x[q].x, (double)x[q].y);
-                const double rho = (double)a.ph.gamma * (pd.x * pd.x + pd.y * pd.y);
+                const double px = (double)v.x, py = (double)v.y;
+                const double rho = (double)a.ph.gamma * (px * px + py * py);
                 Phys<double> phd;
                 phd.inter = a.ph.inter; phd.c_bec = (double)a.ph.c_bec; phd.a_scat = (double)a.ph.a_scat;
                 acc[0] += rho * (double)vext_at(a, idx, ix, iy, iz, it);
                 acc[1] += EDF(phd, rho);
             }
+            own(q) = v;
         }
+        from_cells();
     }
 
     // -------------------------------------------------- Laplacian pair + MID
-    if (a.flags & (F_LAP | F_EKIN)) {
-        C2<R> c[E];
+    if (ops & OP_COPY) {
 #pragma unroll
-        for (int q = 0; q < E; q++) c[q] = x[q];
-        fft<R, N, false, SSTR>(c, sb, t, a.tw);
+        for (int q = 0; q < E; q++) slotB[q * NT + tid] = x[q];
+    }
+    if (a.flags & (F_LAP | F_EKIN)) {
+        fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
         if (a.flags & F_EKIN) {
 #pragma unroll
             for (int q = 0; q < E; q++) {
-                const double w = (double)__ldg(a.ltab + t + T * q);
-                acc[2] += w * ((double)c[q].x * (double)c[q].x + (double)c[q].y * (double)c[q].y);
+                const double w = (double)slt[t + T * q];
+                acc[2] += w * ((double)x[q].x * (double)x[q].x + (double)x[q].y * (double)x[q].y);
             }
         } else {
 #pragma unroll
-            for (int q = 0; q < E; q++) c[q] = cscale(c[q], __ldg(a.ltab + t + T * q));
-            fft<R, N, true, SSTR>(c, sb, t, a.tw);
+            for (int q = 0; q < E; q++) x[q] = cscale(x[q], slt[t + T * q]);
+            fft<R, N, true, SSTR, G>(x, sb, t, stw, bar);
+            if (ops) cp_async_wait_all();
+            if (a.mid == MID_LAP_STORE) {
 #pragma unroll
-            for (int q = 0; q < E; q++) {
-                const size_t idx = base + (size_t)(t + T * q) * estr;
-                if (a.mid == MID_LAP_STORE) {
-                    a.lap[idx] = c[q];
-                } else if (a.mid == MID_LAP_ACC) {
-                    a.lap[idx] = cadd(a.lap[idx], c[q]);
-                } else if (a.mid == MID_QF_VSTEP1) {
-                    const int ix = (int)(idx >> (ly + lz)), iy = (int)((idx >> lz) & ((1u << ly) - 1)),
-                              iz = (int)(idx & ((1u << lz) - 1));
-                    const C2<R> L = cadd(a.lap[idx], c[q]);
-                    const R rho = density(a.ph, x[q]);
+                for (int q = 0; q < E; q++) a.lap[at(q)] = x[q];
+            } else if (a.mid == MID_LAP_ACC) {
+#pragma unroll
+                for (int q = 0; q < E; q++) {
+                    C2<R> l = slotA[q * NT + tid];
+                    if (scale_in) l = cscale(l, s_prev);  // stored from the unscaled psi
+                    a.lap[at(q)] = cadd(l, x[q]);
+                }
+            } else if (a.mid == MID_QF_VSTEP1) {
+                to_cells();
+#pragma unroll 1
+                for (int q = 0; q < E; q++) {
+                    const uint32_t idx = at(q);
+                    int ix, iy, iz;
+                    decode(idx, ix, iy, iz);
+                    const C2<R> L = cadd(slotA[q * NT + tid], own(q));
+                    const C2<R> p = slotB[q * NT + tid];
+                    const R rho = density(a.ph, p);
                     // Im(conj(psi) L) / (rho + eps)   (dev/gpe_engine.cu:916)
-                    const R vqf = (x[q].x * L.y + (-x[q].y) * L.x) / (rho + a.ph.qf_eps);
+                    const R vqf = (p.x * L.y + (-p.y) * L.x) / (rho + a.ph.qf_eps);
                     a.Vqf[idx] = vqf;
                     const R V = (vext_at(a, idx, ix, iy, iz, it) + dEDFdn(a.ph, rho)) + vqf;
                     a.V[idx] = V;
-                    x[q] = cmul(x[q], phase(a.ph, V));
+                    own(q) = cmul(p, phase(a.ph, V));
                 }
+                from_cells();
             }
         }
     }
 
     // ---------------------------------------------------------- kinetic pair
     if (a.flags & F_KIN) {
-        fft<R, N, false, SSTR>(x, sb, t, a.tw);
+        fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
 #pragma unroll
-        for (int q = 0; q < E; q++) x[q] = cmul(x[q], a.ktab[t + T * q]);
-        fft<R, N, true, SSTR>(x, sb, t, a.tw);
+        for (int q = 0; q < E; q++) x[q] = cmul(x[q], skt[t + T * q]);
+        fft<R, N, true, SSTR, G>(x, sb, t, stw, bar);
     }
 
-    // ---------------------------------------------------------------- POST
+    // ------------------------------------------- POST, partial sums, store
     if (a.post != POST_NONE) {
-#pragma unroll
+        if (ops) cp_async_wait_all();
+        to_cells();
+#pragma unroll 1
         for (int q = 0; q < E; q++) {
-            const size_t idx = base + (size_t)(t + T * q) * estr;
-            const int ix = (int)(idx >> (ly + lz)), iy = (int)((idx >> lz) & ((1u << ly) - 1)),
-                      iz = (int)(idx & ((1u << lz) - 1));
+            const uint32_t idx = at(q);
+            C2<R> v = own(q);
             if (a.post == POST_VSTEP2 || a.post == POST_PART12) {
-                R lv = a.V[idx];
-                const C2<R> pp = cmul(x[q], phase(a.ph, lv));
+                int ix, iy, iz;
+                decode(idx, ix, iy, iz);
+                R lv = slotC[q * NT + tid];
+                const C2<R> pp = cmul(v, phase(a.ph, lv));
                 const R rho = density(a.ph, pp);
                 lv = (lv + vext_at(a, idx, ix, iy, iz, it + 1)) + dEDFdn(a.ph, rho);
-                if (a.post == POST_PART12 && (a.flags & F_QF)) lv += a.Vqf[idx];
+                if (a.post == POST_PART12 && (a.flags & F_QF)) lv += slotD[q * NT + tid];
                 lv = (R)0.5 * lv;
                 const C2<R> e = phase(a.ph, lv);
                 if (a.flags & F_AUX_CPLX) reinterpret_cast<C2<R>*>(a.aux)[idx] = e;
                 else reinterpret_cast<R*>(a.aux)[idx] = lv;
-                C2<R> p = a.psi[idx];
-                if (a.flags & F_SCALE_IN) p = cscale(p, s_prev);
-                x[q] = cmul(p, e);
+                C2<R> p = slotA[q * NT + tid];
+                if (scale_in) p = cscale(p, s_prev);
+                v = cmul(p, e);
             } else if (a.post == POST_PART1) {
-                x[q] = cmul(x[q], phase(a.ph, a.V[idx]));
+                v = cmul(v, phase(a.ph, slotC[q * NT + tid]));
             } else if (a.post == POST_VSTEP3) {
                 C2<R> e;
-                if (a.flags & F_AUX_CPLX) e = reinterpret_cast<const C2<R>*>(a.aux)[idx];
-                else e = phase(a.ph, reinterpret_cast<const R*>(a.aux)[idx]);
-                x[q] = cmul(x[q], e);
+                if (a.flags & F_AUX_CPLX) e = slotA[q * NT + tid];
+                else e = phase(a.ph, slotC[q * NT + tid]);
+                v = cmul(v, e);
             }
+            own(q) = v;
         }
+        from_cells();
     }
     if (a.flags & F_REDUCE) {
 #pragma unroll
@@ -334,7 +490,15 @@ pass_kernel(const PassArgs<R> a) {
     }
     if (a.flags & F_STORE) {
 #pragma unroll
-        for (int q = 0; q < E; q++) a.out[base + (size_t)(t + T * q) * estr] = x[q];
+        for (int q = 0; q < E; q++) a.out[at(q)] = x[q];
+    }
+    if (a.flags & F_LAP_OUT) {
+        fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
+#pragma unroll
+        for (int q = 0; q < E; q++) x[q] = cscale(x[q], slt[t + T * q]);
+        fft<R, N, true, SSTR, G>(x, sb, t, stw, bar);
+#pragma unroll
+        for (int q = 0; q < E; q++) a.lap[at(q)] = x[q];
     }
 
     // ------------------------------------------------- cross-CTA finalise

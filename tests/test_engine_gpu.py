@@ -125,7 +125,7 @@ def test_graph_replay_is_bit_identical(cuda_device, gpe_lib):
     assert np.array_equal(e1.get_psi()[1], e2.get_psi()[1])
     n0 = e1.kernel_launches()
     e1.evolve_qf(16)
-    assert e1.kernel_launches() - n0 >= 16 * 8
+    assert e1.kernel_launches() - n0 >= 16 * 7  # 7 fused passes per quantum-friction step
 
 
 def test_normalize_and_norm(cuda_device, gpe_lib):
