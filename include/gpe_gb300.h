@@ -81,6 +81,14 @@ void* gpe_gb_get_stream(const gpe_gb_engine* e);
 int gpe_gb_synchronize(gpe_gb_engine* e);
 /* Number of kernels this engine has launched so far. */
 long long gpe_gb_kernel_launches(const gpe_gb_engine* e);
+/* Measurement aid (no reference counterpart): runs nsteps steps launching
+ * each fused pass directly, with CUDA events around every pass.  For pass p
+ * of the step (p < min(*npass, cap)): ms[p] mean duration, bytes[p] the
+ * arrays it must read and write (algorithmic bytes per launch), axis[p]
+ * (0 x, 1 y, 2 z) and kind[p] (kernel class: 0 kinetic, 1 epilogue,
+ * 2 Laplacian, 3 energy).  Advances psi by nsteps steps like evolve_qf. */
+int gpe_gb_profile_passes(gpe_gb_engine* e, int nsteps, float* ms, double* bytes, int* axis, int* kind, int cap,
+                          int* npass);
 /* 1 to replay each step from a captured CUDA graph (default), 0 to launch directly. */
 int gpe_gb_use_graphs(gpe_gb_engine* e, int enable);
 /* Adds a time-sliced potential: `fields` holds nslices real fields of

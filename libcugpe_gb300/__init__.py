@@ -41,6 +41,7 @@ C_ABI_SYMBOLS = [
     "gpe_gb_get_density", "gpe_gb_get_norm", "gpe_gb_normalize_psi", "gpe_gb_evolve_qf", "gpe_gb_energy",
     "gpe_gb_set_psi_device", "gpe_gb_get_psi_device", "gpe_gb_synchronize", "gpe_gb_kernel_launches",
     "gpe_gb_use_graphs", "gpe_gb_set_potential_slices", "gpe_gb_error_string", "gpe_gb_get_stream",
+    "gpe_gb_profile_passes",
 ]
 
 
@@ -86,6 +87,7 @@ def _lib():
             "gpe_gb_set_potential_slices": (i, [vp, dp, i, i]),
             "gpe_gb_error_string": (ctypes.c_char_p, [i]),
             "gpe_gb_get_stream": (vp, [vp]),
+            "gpe_gb_profile_passes": (i, [vp, i, ctypes.POINTER(ctypes.c_float), dp, ip, ip, i, ip]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -207,6 +209,19 @@ class Engine:
 
     def kernel_launches(self) -> int:
         return int(_lib().gpe_gb_kernel_launches(self._h))
+
+    def profile_passes(self, nsteps: int):
+        """Per-pass mean duration (ms), algorithmic bytes, axis and kernel class over nsteps steps."""
+        cap = 16
+        ms = (ctypes.c_float * cap)()
+        by = (ctypes.c_double * cap)()
+        ax = (ctypes.c_int * cap)()
+        kd = (ctypes.c_int * cap)()
+        npass = ctypes.c_int()
+        _check(_lib().gpe_gb_profile_passes(self._h, int(nsteps), ms, by, ax, kd, cap, ctypes.byref(npass)),
+               "profile_passes")
+        return [{"ms": ms[p], "bytes": by[p], "axis": "xyz"[ax[p]], "kind": ("kin", "epi", "lap", "energy")[kd[p]]}
+                for p in range(min(npass.value, cap))]
 
     def use_graphs(self, enable: bool):
         _check(_lib().gpe_gb_use_graphs(self._h, 1 if enable else 0), "use_graphs")

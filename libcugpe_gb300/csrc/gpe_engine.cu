@@ -411,6 +411,70 @@ static int run_steps(Engine* e, const std::vector<PassDesc>& s, int k) {
     return 0;
 }
 
+// Bytes a pass must move at minimum: every array it reads or writes once
+// (the in/out field, V, V_qf, the corrector factor, the Laplacian).
+static double pass_bytes(const Engine* e, const PassDesc& d) {
+    const double S = (double)e->csize(), r = (double)e->rsize();
+    const double A = (d.flags & F_AUX_CPLX) ? S : r;
+    double b = S;  // read `in`
+    if (d.flags & F_STORE) b += S;
+    if (d.pre == PRE_VSTEP1) b += r;
+    if (d.pre == PRE_PART2) b += S + r + A + ((d.flags & F_QF) ? r : 0.0);
+    if (d.mid == MID_LAP_STORE) b += S;
+    if (d.mid == MID_LAP_ACC) b += 2 * S;
+    if (d.mid == MID_QF_VSTEP1) b += S + 2 * r;
+    if (d.post == POST_VSTEP2 || d.post == POST_PART12) b += r + S + A + ((d.post == POST_PART12) ? r : 0.0);
+    if (d.post == POST_PART1) b += r;
+    if (d.post == POST_VSTEP3) b += A;
+    if (d.flags & F_LAP_OUT) b += S;
+    return b * (double)e->n;
+}
+
+template <typename R>
+static int finish_ite(Engine* e);
+
+// Runs `nsteps` steady steps directly with CUDA events around every pass.
+static int profile_passes(Engine* e, int nsteps, float* ms, double* bytes, int* axis, int* cls, int cap,
+                          int* npass) {
+    if (e->qf_raw != 0.0 && !e->lap_valid) {
+        GPE_RC(run_steps(e, schedule(e, true), 1));
+        e->it += 1;
+        e->lap_valid = true;
+    }
+    const std::vector<PassDesc> s = schedule(e, false);
+    const int np = (int)s.size();
+    *npass = np;
+    std::vector<cudaEvent_t> ev(np + 1);
+    for (auto& x : ev) GPE_CK(cudaEventCreate(&x));
+    std::vector<double> acc(np, 0.0);
+    for (int k = 0; k < nsteps; k++) {
+        for (int p = 0; p < np; p++) {
+            GPE_CK(cudaEventRecord(ev[p], e->st));
+            GPE_RC(e->prec == GPE_PRECISION_FP32 ? launch_desc<float>(e, s[p]) : launch_desc<double>(e, s[p]));
+        }
+        GPE_CK(cudaEventRecord(ev[np], e->st));
+        GPE_CK(cudaEventSynchronize(ev[np]));
+        for (int p = 0; p < np; p++) {
+            float t = 0.f;
+            GPE_CK(cudaEventElapsedTime(&t, ev[p], ev[p + 1]));
+            acc[p] += t;
+        }
+    }
+    for (auto& x : ev) cudaEventDestroy(x);
+    for (int p = 0; p < np && p < cap; p++) {
+        ms[p] = (float)(acc[p] / nsteps);
+        bytes[p] = pass_bytes(e, s[p]);
+        axis[p] = s[p].axis;
+        cls[p] = op_class(s[p].pre, s[p].mid, s[p].post, s[p].flags);
+    }
+    e->it += (unsigned)nsteps;
+    if (e->beta != 0.0) {
+        GPE_RC(e->prec == GPE_PRECISION_FP32 ? finish_ite<float>(e) : finish_ite<double>(e));
+        e->lap_valid = false;
+    }
+    return cuda_rc(cudaStreamSynchronize(e->st));
+}
+
 static void drop_graph(Engine* e) {
     if (e->gexec) cudaGraphExecDestroy(e->gexec);
     e->gexec = nullptr;
@@ -790,6 +854,13 @@ int gpe_gb_synchronize(gpe_gb_engine* h) {
 long long gpe_gb_kernel_launches(const gpe_gb_engine* h) { return h ? h->e.launches : -1; }
 
 void* gpe_gb_get_stream(const gpe_gb_engine* h) { return h ? (void*)h->e.st : nullptr; }
+
+int gpe_gb_profile_passes(gpe_gb_engine* h, int nsteps, float* ms, double* bytes, int* axis, int* kind, int cap,
+                          int* npass) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    if (nsteps <= 0 || !ms || !bytes || !axis || !kind || !npass) return GPE_ERR_ARGUMENT;
+    return gpe::profile_passes(&h->e, nsteps, ms, bytes, axis, kind, cap, npass);
+}
 
 int gpe_gb_use_graphs(gpe_gb_engine* h, int enable) {
     if (!h) return GPE_ERR_NO_ENGINE;

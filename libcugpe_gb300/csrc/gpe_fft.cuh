@@ -134,12 +134,15 @@ __host__ __device__ __forceinline__ constexpr int padp(int p) { return p + (p >>
 template <int N> __host__ __device__ constexpr int padded_len() { return N + N / 16 + (N < 16 ? 1 : 0); }
 
 // Barrier over the G threads that exchange one group of pencils: a warp
-// barrier when the group lies inside one warp, else a named barrier.
+// barrier when the group lies inside one warp, else the CTA barrier (every
+// group of a CTA runs the same stage sequence, so they meet at the same
+// barriers; a CTA barrier keeps the per-CTA barrier count at one).
 template <int G> __device__ __forceinline__ void group_sync(int bar) {
+    (void)bar;
     if constexpr (G <= 32) {
         __syncwarp();
     } else {
-        asm volatile("bar.sync %0, %1;" ::"r"(bar), "n"(G) : "memory");
+        __syncthreads();
     }
 }
 

@@ -8,40 +8,45 @@
 
 namespace gpe {
 
-// Threads per CTA: 128, or one pencil group when a group is larger; a
-// narrow variant (one group or one warp) serves lattices with few pencils.
-template <typename R, int N, int AX> constexpr int wide_nt() {
+// Threads per CTA: 128, or one pencil group when a group is larger.  A
+// lattice with fewer pencils than a CTA holds runs a partial last CTA.
+template <typename R, int N, int AX> constexpr int pass_nt() {
     constexpr int g = PassGeom<R, N, AX, 128>::G;
     return g > 128 ? g : 128;
 }
-template <typename R, int N, int AX> constexpr int narrow_nt() {
-    constexpr int g = (AX == AX_Z) ? 32 : (N / Plan<N>::E) * PassGeom<R, N, AX, 128>::CW;
-    return g < 32 ? 32 : g;
-}
 
-template <typename R, int N, int AX, int NT>
+template <typename R, int N, int AX, int NT, int CLS>
 cudaError_t launch_one(const PassArgs<R>& a, size_t pencils, cudaStream_t st) {
     using Geo = PassGeom<R, N, AX, NT>;
     static bool configured = false;  // per instantiation, single device
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(pass_kernel<R, N, AX, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)Geo::SMEM_MAX);
+        cudaError_t e = cudaFuncSetAttribute(pass_kernel<R, N, AX, NT, CLS>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Geo::SMEM_MAX);
+        if (e != cudaSuccess) return e;
+        // the passes use shared memory, not L1, for reuse: ask for the largest carveout
+        e = cudaFuncSetAttribute(pass_kernel<R, N, AX, NT, CLS>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
         if (e != cudaSuccess) return e;
         configured = true;
     }
-    const unsigned grid = (unsigned)(pencils / Geo::W);
+    const unsigned grid = (unsigned)((pencils + Geo::W - 1) / Geo::W);
     const size_t smem = Geo::SMEM_BASE + slot_bytes<R>(staged_ops(a.mid, a.post, a.flags), Geo::E * NT);
-    pass_kernel<R, N, AX, NT><<<grid, NT, smem, st>>>(a);
+    PassArgs<R> b = a;
+    b.npencils = (uint32_t)pencils;
+    pass_kernel<R, N, AX, NT, CLS><<<grid, NT, smem, st>>>(b);
     return cudaGetLastError();
 }
 
 template <typename R, int N, int AX>
 cudaError_t launch_ax(const PassArgs<R>& a, size_t pencils, cudaStream_t st, unsigned* grid_out) {
-    constexpr int NW = wide_nt<R, N, AX>(), NN = narrow_nt<R, N, AX>();
-    constexpr int WW = PassGeom<R, N, AX, NW>::W, WN = PassGeom<R, N, AX, NN>::W;
-    if (pencils % WW == 0) { *grid_out = (unsigned)(pencils / WW); return launch_one<R, N, AX, NW>(a, pencils, st); }
-    if (pencils % WN == 0) { *grid_out = (unsigned)(pencils / WN); return launch_one<R, N, AX, NN>(a, pencils, st); }
-    return cudaErrorInvalidValue;
+    constexpr int NT = pass_nt<R, N, AX>();
+    *grid_out = (unsigned)((pencils + PassGeom<R, N, AX, NT>::W - 1) / PassGeom<R, N, AX, NT>::W);
+    switch (op_class(a.pre, a.mid, a.post, a.flags)) {
+        case C_KIN: return launch_one<R, N, AX, NT, C_KIN>(a, pencils, st);
+        case C_EPI: return launch_one<R, N, AX, NT, C_EPI>(a, pencils, st);
+        case C_LAP: return launch_one<R, N, AX, NT, C_LAP>(a, pencils, st);
+        default: return launch_one<R, N, AX, NT, C_EN>(a, pencils, st);
+    }
 }
 
 template <typename R, int N>

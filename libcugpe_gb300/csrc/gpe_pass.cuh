@@ -98,6 +98,7 @@ struct PassArgs {
     int lx, ly, lz;      // log2 of the lattice sides
     double npart, dt;
     int red_slot;
+    uint32_t npencils;   // pencils along this pass's axis
     uint32_t flags;
     int pre, mid, post;
     Phys<R> ph;
@@ -243,36 +244,43 @@ struct PassGeom {
     static_assert(NT % G == 0 && NT % 32 == 0, "threads per CTA must hold whole groups");
 };
 
-template <typename R, int N, int AX, int NT>
+// Kernel classes: each instantiation compiles only the code its passes use,
+// which keeps register use and instruction footprint down.
+enum : int { C_KIN = 0, C_EPI = 1, C_LAP = 2, C_EN = 3 };
+
+__host__ __device__ inline int op_class(int pre, int mid, int post, uint32_t flags) {
+    (void)mid;
+    if (flags & F_EKIN) return C_EN;
+    if (flags & F_LAP) return C_LAP;
+    if (pre != PRE_NONE || post != POST_NONE ||
+        (flags & (F_LAP_OUT | F_REDUCE | F_FIN_STEP | F_FIN_S2 | F_FIN_RED)))
+        return C_EPI;
+    return C_KIN;
+}
+
+template <typename R, int N, int AX, int NT, int CLS>
 __global__ void __launch_bounds__(NT, PassGeom<R, N, AX, NT>::MINB)
 pass_kernel(const PassArgs<R> a) {
     using Geo = PassGeom<R, N, AX, NT>;
     constexpr int E = Geo::E, T = Geo::T, CW = Geo::CW, G = Geo::G, W = Geo::W, ROW = Geo::ROW;
     constexpr int SSTR = (AX == AX_Z) ? 1 : CW;
+    constexpr bool FIN = (CLS == C_EPI || CLS == C_EN);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C2<R>* stw = reinterpret_cast<C2<R>*>(smem_raw);
     C2<R>* skt = stw + Geo::TW;
     R* slt = reinterpret_cast<R*>(skt + N);
     C2<R>* sx = reinterpret_cast<C2<R>*>(smem_raw + Geo::TAB_BYTES);
-    __shared__ double sred[NT / 32][NRED];
+    __shared__ double sred[FIN ? NT / 32 : 1][NRED];
     __shared__ bool last_cta;
 
     const int tid = threadIdx.x;
     for (int i = tid; i < Geo::TW; i += NT) stw[i] = a.tw[i];
-    for (int i = tid; i < N; i += NT) {
-        skt[i] = a.ktab[i];
-        slt[i] = a.ltab[i];
+    if constexpr (CLS != C_EN) {
+        for (int i = tid; i < N; i += NT) skt[i] = a.ktab[i];
     }
-    // staged operand slots (see staged_ops)
-    const uint32_t ops = staged_ops(a.mid, a.post, a.flags);
-    unsigned char* sop = smem_raw + Geo::SMEM_BASE;
-    C2<R>* slotA = reinterpret_cast<C2<R>*>(sop);
-    if (ops & (OP_PSI | OP_LAP | OP_AUXC)) sop += (size_t)E * NT * sizeof(C2<R>);
-    C2<R>* slotB = reinterpret_cast<C2<R>*>(sop);
-    if (ops & OP_COPY) sop += (size_t)E * NT * sizeof(C2<R>);
-    R* slotC = reinterpret_cast<R*>(sop);
-    if (ops & (OP_V | OP_AUXR)) sop += (size_t)E * NT * sizeof(R);
-    R* slotD = reinterpret_cast<R*>(sop);
+    if constexpr (CLS != C_KIN) {
+        for (int i = tid; i < N; i += NT) slt[i] = a.ltab[i];
+    }
 
     int pl, t, bar;
     C2<R>* sb;
@@ -291,8 +299,10 @@ pass_kernel(const PassArgs<R> a) {
         bar = 1 + gi;
     }
 
-    // 32-bit point indices: the largest lattice (512^3) has 2^27 points
+    // 32-bit point indices: the largest lattice (512^3) has 2^27 points.
+    // CTAs past the last pencil (small lattices) compute on zeros and store nothing.
     const uint32_t gp = blockIdx.x * (uint32_t)W + pl;  // pencil id
+    const bool valid = gp < a.npencils;
     const int ly = a.ly, lz = a.lz;
     uint32_t base, lstr;  // first point of the pencil, log2 of the point stride
     if constexpr (AX == AX_Z) { base = gp << lz; lstr = 0; }
@@ -315,28 +325,48 @@ pass_kernel(const PassArgs<R> a) {
 
     C2<R> x[E];
 #pragma unroll
-    for (int q = 0; q < E; q++) x[q] = ldc(a.in + at(q));
-    if (ops) {
-        const void* srcA = (ops & OP_PSI) ? (const void*)a.psi : (ops & OP_LAP) ? (const void*)a.lap : a.aux;
-        const void* srcC = (ops & OP_V) ? (const void*)a.V : a.aux;
+    for (int q = 0; q < E; q++) x[q] = valid ? ldc(a.in + at(q)) : mk<R>((R)0, (R)0);
+
+    // staged operand slots (see staged_ops)
+    uint32_t ops = 0;
+    C2<R>* slotA = nullptr;
+    C2<R>* slotB = nullptr;
+    R* slotC = nullptr;
+    R* slotD = nullptr;
+    if constexpr (CLS == C_EPI || CLS == C_LAP) {
+        ops = staged_ops(a.mid, a.post, a.flags);
+        unsigned char* sop = smem_raw + Geo::SMEM_BASE;
+        slotA = reinterpret_cast<C2<R>*>(sop);
+        if (ops & (OP_PSI | OP_LAP | OP_AUXC)) sop += (size_t)E * NT * sizeof(C2<R>);
+        slotB = reinterpret_cast<C2<R>*>(sop);
+        if (ops & OP_COPY) sop += (size_t)E * NT * sizeof(C2<R>);
+        slotC = reinterpret_cast<R*>(sop);
+        if (ops & (OP_V | OP_AUXR)) sop += (size_t)E * NT * sizeof(R);
+        slotD = reinterpret_cast<R*>(sop);
+        if (ops && valid) {
+            const void* srcA = (ops & OP_PSI) ? (const void*)a.psi : (ops & OP_LAP) ? (const void*)a.lap : a.aux;
+            const void* srcC = (ops & OP_V) ? (const void*)a.V : a.aux;
 #pragma unroll
-        for (int q = 0; q < E; q++) {
-            const uint32_t idx = at(q);
-            if (ops & (OP_PSI | OP_LAP | OP_AUXC))
-                cp_async(slotA + q * NT + tid, reinterpret_cast<const C2<R>*>(srcA) + idx, sizeof(C2<R>));
-            if (ops & (OP_V | OP_AUXR)) cp_async(slotC + q * NT + tid, reinterpret_cast<const R*>(srcC) + idx, sizeof(R));
-            if (ops & OP_VQF) cp_async(slotD + q * NT + tid, a.Vqf + idx, sizeof(R));
+            for (int q = 0; q < E; q++) {
+                const uint32_t idx = at(q);
+                if (ops & (OP_PSI | OP_LAP | OP_AUXC))
+                    cp_async(slotA + q * NT + tid, reinterpret_cast<const C2<R>*>(srcA) + idx, sizeof(C2<R>));
+                if (ops & (OP_V | OP_AUXR))
+                    cp_async(slotC + q * NT + tid, reinterpret_cast<const R*>(srcC) + idx, sizeof(R));
+                if (ops & OP_VQF) cp_async(slotD + q * NT + tid, a.Vqf + idx, sizeof(R));
+            }
         }
         cp_async_commit();
     }
+    if (scale_in) {
 #pragma unroll
-    for (int q = 0; q < E; q++)
-        if (scale_in) x[q] = cscale(x[q], s_prev);
+        for (int q = 0; q < E; q++) x[q] = cscale(x[q], s_prev);
+    }
     __syncthreads();  // tables staged
 
     double acc[NRED] = {0.0, 0.0, 0.0};
 
-    // The pointwise ops below run in rolled loops over this thread's own
+    // The heavy pointwise ops run in rolled loops over this thread's own
     // cells of the exchange buffer (positions t + T*q, which only this thread
     // reads between transforms; every exchange starts with a group barrier),
     // so their transcendental-heavy bodies appear once in the instruction
@@ -352,62 +382,68 @@ pass_kernel(const PassArgs<R> a) {
     };
 
     // ---------------------------------------------------------------- PRE
-    if (a.pre != PRE_NONE) {
-        const R s2 = (R)dyn->s2;
-        to_cells();
+    if constexpr (CLS == C_EPI || CLS == C_EN) {
+        if (a.pre != PRE_NONE && valid) {
+            const R s2 = (R)dyn->s2;
+            to_cells();
 #pragma unroll 1
-        for (int q = 0; q < E; q++) {
-            const uint32_t idx = at(q);
-            int ix, iy, iz;
-            decode(idx, ix, iy, iz);
-            C2<R> v = own(q);
-            if (a.pre == PRE_VSTEP1) {
-                const R rho = density(a.ph, v);
-                const R V = vext_at(a, idx, ix, iy, iz, it) + dEDFdn(a.ph, rho);
-                a.V[idx] = V;
-                v = cmul(v, phase(a.ph, V));
-            } else if (a.pre == PRE_PART2) {
-                C2<R> p2 = a.psi2[idx];
-                if (a.flags & F_SCALE_PSI2) p2 = cscale(p2, s2);
-                const R rho = density(a.ph, p2);
-                R lv = (a.V[idx] + vext_at(a, idx, ix, iy, iz, it + 1)) + dEDFdn(a.ph, rho);
-                if (a.flags & F_QF) lv += a.Vqf[idx];
-                lv = (R)0.5 * lv;
-                const C2<R> e = phase(a.ph, lv);
-                if (a.flags & F_AUX_CPLX) reinterpret_cast<C2<R>*>(a.aux)[idx] = e;
-                else reinterpret_cast<R*>(a.aux)[idx] = lv;
-                v = cmul(v, e);
-            } else if (a.pre == PRE_ENERGY) {
-                const double px = (double)v.x, py = (double)v.y;
-                const double rho = (double)a.ph.gamma * (px * px + py * py);
-                Phys<double> phd;
-                phd.inter = a.ph.inter; phd.c_bec = (double)a.ph.c_bec; phd.a_scat = (double)a.ph.a_scat;
-                acc[0] += rho * (double)vext_at(a, idx, ix, iy, iz, it);
-                acc[1] += EDF(phd, rho);
+            for (int q = 0; q < E; q++) {
+                const uint32_t idx = at(q);
+                int ix, iy, iz;
+                decode(idx, ix, iy, iz);
+                C2<R> v = own(q);
+                if (CLS == C_EPI && a.pre == PRE_VSTEP1) {
+                    const R rho = density(a.ph, v);
+                    const R V = vext_at(a, idx, ix, iy, iz, it) + dEDFdn(a.ph, rho);
+                    a.V[idx] = V;
+                    v = cmul(v, phase(a.ph, V));
+                } else if (CLS == C_EPI && a.pre == PRE_PART2) {
+                    C2<R> p2 = a.psi2[idx];
+                    if (a.flags & F_SCALE_PSI2) p2 = cscale(p2, s2);
+                    const R rho = density(a.ph, p2);
+                    R lv = (a.V[idx] + vext_at(a, idx, ix, iy, iz, it + 1)) + dEDFdn(a.ph, rho);
+                    if (a.flags & F_QF) lv += a.Vqf[idx];
+                    lv = (R)0.5 * lv;
+                    const C2<R> e = phase(a.ph, lv);
+                    if (a.flags & F_AUX_CPLX) reinterpret_cast<C2<R>*>(a.aux)[idx] = e;
+                    else reinterpret_cast<R*>(a.aux)[idx] = lv;
+                    v = cmul(v, e);
+                } else if (CLS == C_EN && a.pre == PRE_ENERGY) {
+                    const double px = (double)v.x, py = (double)v.y;
+                    const double rho = (double)a.ph.gamma * (px * px + py * py);
+                    Phys<double> phd;
+                    phd.inter = a.ph.inter; phd.c_bec = (double)a.ph.c_bec; phd.a_scat = (double)a.ph.a_scat;
+                    acc[0] += rho * (double)vext_at(a, idx, ix, iy, iz, it);
+                    acc[1] += EDF(phd, rho);
+                }
+                own(q) = v;
             }
-            own(q) = v;
+            from_cells();
         }
-        from_cells();
+    }
+
+    // ------------------------------------------------- energy: forward only
+    if constexpr (CLS == C_EN) {
+        fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
+#pragma unroll
+        for (int q = 0; q < E; q++) {
+            const double w = (double)slt[t + T * q];
+            acc[2] += w * ((double)x[q].x * (double)x[q].x + (double)x[q].y * (double)x[q].y);
+        }
     }
 
     // -------------------------------------------------- Laplacian pair + MID
-    if (ops & OP_COPY) {
+    if constexpr (CLS == C_LAP) {
+        if (ops & OP_COPY) {
 #pragma unroll
-        for (int q = 0; q < E; q++) slotB[q * NT + tid] = x[q];
-    }
-    if (a.flags & (F_LAP | F_EKIN)) {
+            for (int q = 0; q < E; q++) slotB[q * NT + tid] = x[q];
+        }
         fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
-        if (a.flags & F_EKIN) {
 #pragma unroll
-            for (int q = 0; q < E; q++) {
-                const double w = (double)slt[t + T * q];
-                acc[2] += w * ((double)x[q].x * (double)x[q].x + (double)x[q].y * (double)x[q].y);
-            }
-        } else {
-#pragma unroll
-            for (int q = 0; q < E; q++) x[q] = cscale(x[q], slt[t + T * q]);
-            fft<R, N, true, SSTR, G>(x, sb, t, stw, bar);
-            if (ops) cp_async_wait_all();
+        for (int q = 0; q < E; q++) x[q] = cscale(x[q], slt[t + T * q]);
+        fft<R, N, true, SSTR, G>(x, sb, t, stw, bar);
+        cp_async_wait_all();
+        if (valid) {
             if (a.mid == MID_LAP_STORE) {
 #pragma unroll
                 for (int q = 0; q < E; q++) a.lap[at(q)] = x[q];
@@ -441,80 +477,92 @@ pass_kernel(const PassArgs<R> a) {
     }
 
     // ---------------------------------------------------------- kinetic pair
-    if (a.flags & F_KIN) {
-        fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
+    if constexpr (CLS != C_EN) {
+        if (CLS != C_LAP || (a.flags & F_KIN)) {
+            fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
 #pragma unroll
-        for (int q = 0; q < E; q++) x[q] = cmul(x[q], skt[t + T * q]);
-        fft<R, N, true, SSTR, G>(x, sb, t, stw, bar);
+            for (int q = 0; q < E; q++) x[q] = cmul(x[q], skt[t + T * q]);
+            fft<R, N, true, SSTR, G>(x, sb, t, stw, bar);
+        }
     }
 
     // ------------------------------------------- POST, partial sums, store
-    if (a.post != POST_NONE) {
-        if (ops) cp_async_wait_all();
-        to_cells();
+    if constexpr (CLS == C_EPI) {
+        if (a.post != POST_NONE && valid) {
+            cp_async_wait_all();
+            to_cells();
 #pragma unroll 1
-        for (int q = 0; q < E; q++) {
-            const uint32_t idx = at(q);
-            C2<R> v = own(q);
-            if (a.post == POST_VSTEP2 || a.post == POST_PART12) {
-                int ix, iy, iz;
-                decode(idx, ix, iy, iz);
-                R lv = slotC[q * NT + tid];
-                const C2<R> pp = cmul(v, phase(a.ph, lv));
-                const R rho = density(a.ph, pp);
-                lv = (lv + vext_at(a, idx, ix, iy, iz, it + 1)) + dEDFdn(a.ph, rho);
-                if (a.post == POST_PART12 && (a.flags & F_QF)) lv += slotD[q * NT + tid];
-                lv = (R)0.5 * lv;
-                const C2<R> e = phase(a.ph, lv);
-                if (a.flags & F_AUX_CPLX) reinterpret_cast<C2<R>*>(a.aux)[idx] = e;
-                else reinterpret_cast<R*>(a.aux)[idx] = lv;
-                C2<R> p = slotA[q * NT + tid];
-                if (scale_in) p = cscale(p, s_prev);
-                v = cmul(p, e);
-            } else if (a.post == POST_PART1) {
-                v = cmul(v, phase(a.ph, slotC[q * NT + tid]));
-            } else if (a.post == POST_VSTEP3) {
-                C2<R> e;
-                if (a.flags & F_AUX_CPLX) e = slotA[q * NT + tid];
-                else e = phase(a.ph, slotC[q * NT + tid]);
-                v = cmul(v, e);
+            for (int q = 0; q < E; q++) {
+                const uint32_t idx = at(q);
+                C2<R> v = own(q);
+                if (a.post == POST_VSTEP2 || a.post == POST_PART12) {
+                    int ix, iy, iz;
+                    decode(idx, ix, iy, iz);
+                    R lv = slotC[q * NT + tid];
+                    const C2<R> pp = cmul(v, phase(a.ph, lv));
+                    const R rho = density(a.ph, pp);
+                    lv = (lv + vext_at(a, idx, ix, iy, iz, it + 1)) + dEDFdn(a.ph, rho);
+                    if (a.post == POST_PART12 && (a.flags & F_QF)) lv += slotD[q * NT + tid];
+                    lv = (R)0.5 * lv;
+                    const C2<R> e = phase(a.ph, lv);
+                    if (a.flags & F_AUX_CPLX) reinterpret_cast<C2<R>*>(a.aux)[idx] = e;
+                    else reinterpret_cast<R*>(a.aux)[idx] = lv;
+                    C2<R> p = slotA[q * NT + tid];
+                    if (scale_in) p = cscale(p, s_prev);
+                    v = cmul(p, e);
+                } else if (a.post == POST_PART1) {
+                    v = cmul(v, phase(a.ph, slotC[q * NT + tid]));
+                } else if (a.post == POST_VSTEP3) {
+                    C2<R> e;
+                    if (a.flags & F_AUX_CPLX) e = slotA[q * NT + tid];
+                    else e = phase(a.ph, slotC[q * NT + tid]);
+                    v = cmul(v, e);
+                }
+                own(q) = v;
             }
-            own(q) = v;
+            from_cells();
         }
-        from_cells();
+        if (a.flags & F_REDUCE) {
+#pragma unroll
+            for (int q = 0; q < E; q++)
+                acc[0] += (double)a.ph.gamma * ((double)x[q].x * (double)x[q].x + (double)x[q].y * (double)x[q].y);
+        }
     }
-    if (a.flags & F_REDUCE) {
+    if constexpr (CLS != C_EN) {
+        if ((a.flags & F_STORE) && valid) {
 #pragma unroll
-        for (int q = 0; q < E; q++)
-            acc[0] += (double)a.ph.gamma * ((double)x[q].x * (double)x[q].x + (double)x[q].y * (double)x[q].y);
+            for (int q = 0; q < E; q++) a.out[at(q)] = x[q];
+        }
     }
-    if (a.flags & F_STORE) {
+    if constexpr (CLS == C_EPI) {
+        if (a.flags & F_LAP_OUT) {
+            fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
 #pragma unroll
-        for (int q = 0; q < E; q++) a.out[at(q)] = x[q];
-    }
-    if (a.flags & F_LAP_OUT) {
-        fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
+            for (int q = 0; q < E; q++) x[q] = cscale(x[q], slt[t + T * q]);
+            fft<R, N, true, SSTR, G>(x, sb, t, stw, bar);
+            if (valid) {
 #pragma unroll
-        for (int q = 0; q < E; q++) x[q] = cscale(x[q], slt[t + T * q]);
-        fft<R, N, true, SSTR, G>(x, sb, t, stw, bar);
-#pragma unroll
-        for (int q = 0; q < E; q++) a.lap[at(q)] = x[q];
+                for (int q = 0; q < E; q++) a.lap[at(q)] = x[q];
+            }
+        }
     }
 
     // ------------------------------------------------- cross-CTA finalise
-    if (a.flags & (F_FIN_S2 | F_FIN_STEP | F_FIN_RED)) {
-        block_sum<NT>(acc, sred);
-        if (tid == 0) {
+    if constexpr (FIN) {
+        if (a.flags & (F_FIN_S2 | F_FIN_STEP | F_FIN_RED)) {
+            block_sum<NT>(acc, sred);
+            if (tid == 0) {
 #pragma unroll
-            for (int r = 0; r < NRED; r++) a.partials[(size_t)blockIdx.x * NRED + r] = acc[r];
-            __threadfence();
-            const unsigned prev = atomicAdd(&a.dyn->ticket, 1u);
-            last_cta = (prev == gridDim.x - 1);
-        }
-        __syncthreads();
-        if (last_cta) {
-            __threadfence();
-            finalize<R, NT>(a, sred);
+                for (int r = 0; r < NRED; r++) a.partials[(size_t)blockIdx.x * NRED + r] = acc[r];
+                __threadfence();
+                const unsigned prev = atomicAdd(&a.dyn->ticket, 1u);
+                last_cta = (prev == gridDim.x - 1);
+            }
+            __syncthreads();
+            if (last_cta) {
+                __threadfence();
+                finalize<R, NT>(a, sred);
+            }
         }
     }
 }
