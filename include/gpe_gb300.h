@@ -29,6 +29,7 @@ extern "C" {
 #define GPE_ERR_NO_ENGINE (-11)        /* null handle / engine not created */
 #define GPE_ERR_ARGUMENT (-12)         /* null pointer or bad value */
 #define GPE_ERR_FUNCTIONAL (-13)       /* unknown interactions code */
+#define GPE_ERR_NOALLOC_SIZE (-14)     /* more points than gpe_gb_norm_noalloc's scratch serves */
 #define GPE_ERR_NOT_IMPLEMENTED (-98)  /* reference entry point outside this engine */
 
 #define GPE_PRECISION_FP64 0 /* plain FP64 drop-in */
@@ -95,6 +96,22 @@ int gpe_gb_use_graphs(gpe_gb_engine* e, int enable);
  * nx*ny*nz doubles; step `it` uses slice min(it / steps_per_slice, nslices-1)
  * on top of the harmonic trap.  NULL removes it. */
 int gpe_gb_set_potential_slices(gpe_gb_engine* e, const double* fields, int nslices, int steps_per_slice);
+/* Allocation-free norm (no counterpart in the reference library).
+ * For callers that cannot allocate device memory when they need the norm:
+ * code running while its stream is captured into a CUDA graph, applications
+ * whose own pool owns all device memory, plugins in hosts that forbid
+ * allocations after start-up.  Writes sum gamma |psi|^2 over n points of the
+ * device array `psi` (complex128 for GPE_PRECISION_FP64, complex64 for
+ * GPE_PRECISION_FP32) into the device double `norm_out`, ordered on
+ * `stream` (NULL = legacy default stream), and allocates nothing: its
+ * scratch is a fixed 4.25 KiB device array inside the library, held by every
+ * GPU that loads the library until the process exits.  At most 2^27 points
+ * (512^3); more returns GPE_ERR_NOALLOC_SIZE.  The first call on a device
+ * looks up the scratch address (cudaGetSymbolAddress) and must come before
+ * any stream capture.  All calls share the scratch: calls whose kernels can
+ * overlap on the GPU (different streams, or host threads) race and must be
+ * serialised by the caller. */
+int gpe_gb_norm_noalloc(const void* psi, int precision, long long n, double gamma, double* norm_out, void* stream);
 /* Message for a return code. */
 const char* gpe_gb_error_string(int code);
 

@@ -32,6 +32,7 @@ ERR_LATTICE = -10
 ERR_NO_ENGINE = -11
 ERR_ARGUMENT = -12
 ERR_FUNCTIONAL = -13
+ERR_NOALLOC_SIZE = -14
 ERR_NOT_IMPLEMENTED = -98
 
 # entry points declared in include/gpe_gb300.h
@@ -41,7 +42,7 @@ C_ABI_SYMBOLS = [
     "gpe_gb_get_density", "gpe_gb_get_norm", "gpe_gb_normalize_psi", "gpe_gb_evolve_qf", "gpe_gb_energy",
     "gpe_gb_set_psi_device", "gpe_gb_get_psi_device", "gpe_gb_synchronize", "gpe_gb_kernel_launches",
     "gpe_gb_use_graphs", "gpe_gb_set_potential_slices", "gpe_gb_error_string", "gpe_gb_get_stream",
-    "gpe_gb_profile_passes",
+    "gpe_gb_profile_passes", "gpe_gb_norm_noalloc",
 ]
 
 
@@ -87,6 +88,7 @@ def _lib():
             "gpe_gb_set_potential_slices": (i, [vp, dp, i, i]),
             "gpe_gb_error_string": (ctypes.c_char_p, [i]),
             "gpe_gb_get_stream": (vp, [vp]),
+            "gpe_gb_norm_noalloc": (i, [vp, i, ctypes.c_longlong, d, vp, vp]),
             "gpe_gb_profile_passes": (i, [vp, i, ctypes.POINTER(ctypes.c_float), dp, ip, ip, i, ip]),
         }
         for name, (res, args) in sig.items():

@@ -40,6 +40,7 @@ def _sources():
                     fh.write(text)
             units.append(path)
     units.append(os.path.join(CSRC, "gpe_engine.cu"))
+    units.append(os.path.join(CSRC, "gpe_noalloc.cu"))
     units.append(os.path.join(CSRC, "gpe_dropin.cpp"))
     return units
 
