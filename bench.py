@@ -97,13 +97,15 @@ class Clocks:
 
 
 def dist_setup():
+    """Replicas only: one independent condensate per rank, no data-path collective."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if ws > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     return ws, rank, local
 
@@ -119,9 +121,15 @@ def max_over_ranks(ws, x):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def whole_job_rate(ws, units_per_rank, seconds_this_rank):
+    """Units all ranks processed / the slowest rank's time (weak scaling over replicas)."""
+    return ws * units_per_rank / max_over_ranks(ws, seconds_this_rank)
 
 
 def traffic_from_profiles(n):
@@ -309,16 +317,15 @@ def main():
     barrier(ws)
     with Clocks(local) as clk:
         t32, launches = time_blocks(e32, args.block, args.steps, args.warmup, flush, torch)
+    value = whole_job_rate(ws, args.steps * args.block, t32)
     t32 = max_over_ranks(ws, t32)
-    value = ws * args.steps * args.block / t32
     # per-pass kernel times (CUDA events around each fused pass, engine stream)
     passes = e32.profile_passes(20)
 
     host = torch.empty(w.shape + (2,), dtype=torch.float64, pin_memory=True).numpy().view(np.complex128)[..., 0]
     host[...] = psi
     te2e = time_e2e(e32, args.block, max(2, args.steps // 2), host, flush, torch)
-    te2e = max_over_ranks(ws, te2e)
-    e2e_value = ws * max(2, args.steps // 2) * args.block / te2e
+    e2e_value = whole_job_rate(ws, max(2, args.steps // 2) * args.block, te2e)
 
     extras = {}
     if not args.no_extras and rank == 0:

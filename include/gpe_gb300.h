@@ -70,6 +70,21 @@ int gpe_gb_evolve_qf(gpe_gb_engine* e, int nt, double* chemical_potential);
 /* gpe_energy (dev/gpe_engine.cu:1669) */
 int gpe_gb_energy(gpe_gb_engine* e, double* t, double* ekin, double* eint, double* eext);
 
+/* gpe_set_vortex (dev/gpe_engine.cu:465): vortex line along z through
+ * (x0, y0) in lattice offsets from the box centre, charge q. */
+int gpe_gb_set_vortex(gpe_gb_engine* e, double x0, double y0, int q);
+/* gpe_get_phase (dev/gpe_engine.cu:572): phase = arg psi kept for
+ * gpe_gb_evolve_enforced_phase; copied to `phase` (nx*ny*nz doubles) if not NULL. */
+int gpe_gb_get_phase(gpe_gb_engine* e, double* phase);
+/* gpe_set_phase (dev/gpe_engine.cu:561) */
+int gpe_gb_set_phase(gpe_gb_engine* e, const double* phase);
+/* gpe_evolve_vortex (method 1), gpe_evolve_vortex2 (2), gpe_evolve_vortex3 (3)
+ * (dev/gpe_engine.cu:1115, 1207, 1299): the vortex phase is imposed at the
+ * start of every step; method 2 leaves points with |psi| <= 1e-15 alone. */
+int gpe_gb_evolve_vortex(gpe_gb_engine* e, int nt, double* chemical_potential, int method);
+/* gpe_evolve_enforced_phase (dev/gpe_engine.cu:1390) */
+int gpe_gb_evolve_enforced_phase(gpe_gb_engine* e, int nt, double* chemical_potential);
+
 /* Device-resident I/O (no reference counterpart; used when the caller keeps
  * the wavefunction in GPU memory): psi is a device pointer to nx*ny*nz
  * complex128 values. */

@@ -42,7 +42,8 @@ C_ABI_SYMBOLS = [
     "gpe_gb_get_density", "gpe_gb_get_norm", "gpe_gb_normalize_psi", "gpe_gb_evolve_qf", "gpe_gb_energy",
     "gpe_gb_set_psi_device", "gpe_gb_get_psi_device", "gpe_gb_synchronize", "gpe_gb_kernel_launches",
     "gpe_gb_use_graphs", "gpe_gb_set_potential_slices", "gpe_gb_error_string", "gpe_gb_get_stream",
-    "gpe_gb_profile_passes", "gpe_gb_norm_noalloc",
+    "gpe_gb_profile_passes", "gpe_gb_norm_noalloc", "gpe_gb_set_vortex", "gpe_gb_get_phase", "gpe_gb_set_phase",
+    "gpe_gb_evolve_vortex", "gpe_gb_evolve_enforced_phase",
 ]
 
 
@@ -89,6 +90,11 @@ def _lib():
             "gpe_gb_error_string": (ctypes.c_char_p, [i]),
             "gpe_gb_get_stream": (vp, [vp]),
             "gpe_gb_norm_noalloc": (i, [vp, i, ctypes.c_longlong, d, vp, vp]),
+            "gpe_gb_set_vortex": (i, [vp, d, d, i]),
+            "gpe_gb_get_phase": (i, [vp, dp]),
+            "gpe_gb_set_phase": (i, [vp, dp]),
+            "gpe_gb_evolve_vortex": (i, [vp, i, dp, i]),
+            "gpe_gb_evolve_enforced_phase": (i, [vp, i, dp]),
             "gpe_gb_profile_passes": (i, [vp, i, ctypes.POINTER(ctypes.c_float), dp, ip, ip, i, ip]),
         }
         for name, (res, args) in sig.items():
@@ -195,6 +201,28 @@ class Engine:
     def evolve_qf(self, nt):
         mu = ctypes.c_double(0.0)
         _check(_lib().gpe_gb_evolve_qf(self._h, int(nt), ctypes.byref(mu)), "evolve_qf")
+        return mu.value
+
+    def set_vortex(self, x0, y0, q=1):
+        _check(_lib().gpe_gb_set_vortex(self._h, float(x0), float(y0), int(q)), "set_vortex")
+
+    def get_phase(self):
+        out = np.empty(self.shape, dtype=np.float64)
+        _check(_lib().gpe_gb_get_phase(self._h, _dp(out)), "get_phase")
+        return out
+
+    def set_phase(self, phase):
+        p = np.ascontiguousarray(phase, dtype=np.float64).reshape(self.shape)
+        _check(_lib().gpe_gb_set_phase(self._h, _dp(p)), "set_phase")
+
+    def evolve_vortex(self, nt, method=1):
+        mu = ctypes.c_double(0.0)
+        _check(_lib().gpe_gb_evolve_vortex(self._h, int(nt), ctypes.byref(mu), int(method)), "evolve_vortex")
+        return mu.value
+
+    def evolve_enforced_phase(self, nt):
+        mu = ctypes.c_double(0.0)
+        _check(_lib().gpe_gb_evolve_enforced_phase(self._h, int(nt), ctypes.byref(mu)), "evolve_enforced_phase")
         return mu.value
 
     def energy(self):

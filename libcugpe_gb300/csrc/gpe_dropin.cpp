@@ -86,15 +86,16 @@ int gpe_evolve(int nt) {
 
 void gpe_print_potential_type() { printf("%s\n", "HARMONIC POTENTIAL\n"); }
 
+int gpe_set_vortex(const double x0, const double y0, const int8_t Q) { return gpe_gb_set_vortex(g_engine, x0, y0, Q); }
+int gpe_get_phase(double* h_phase) { return gpe_gb_get_phase(g_engine, h_phase); }
+int gpe_set_phase(double* h_phase) { return gpe_gb_set_phase(g_engine, h_phase); }
+int gpe_evolve_vortex(int nt, double* mu) { return gpe_gb_evolve_vortex(g_engine, nt, mu, 1); }
+int gpe_evolve_vortex2(int nt, double* mu) { return gpe_gb_evolve_vortex(g_engine, nt, mu, 2); }
+int gpe_evolve_vortex3(int nt, double* mu) { return gpe_gb_evolve_vortex(g_engine, nt, mu, 3); }
+int gpe_evolve_enforced_phase(int nt, double* mu) { return gpe_gb_evolve_enforced_phase(g_engine, nt, mu); }
+
 // Reference entry points outside the split-step evolution of this engine.
-int gpe_set_vortex(const double, const double, const int8_t) { return GPE_ERR_NOT_IMPLEMENTED; }
-int gpe_get_phase(double*) { return GPE_ERR_NOT_IMPLEMENTED; }
-int gpe_set_phase(double*) { return GPE_ERR_NOT_IMPLEMENTED; }
 int gpe_get_currents(double*, double*, double*, double*) { return GPE_ERR_NOT_IMPLEMENTED; }
-int gpe_evolve_vortex(int, double*) { return GPE_ERR_NOT_IMPLEMENTED; }
-int gpe_evolve_vortex2(int, double*) { return GPE_ERR_NOT_IMPLEMENTED; }
-int gpe_evolve_vortex3(int, double*) { return GPE_ERR_NOT_IMPLEMENTED; }
-int gpe_evolve_enforced_phase(int, double*) { return GPE_ERR_NOT_IMPLEMENTED; }
 int gpe_evolve_dipolar(int) { return GPE_ERR_NOT_IMPLEMENTED; }
 int gpe_evolve_dipolar(int, double*) { return GPE_ERR_NOT_IMPLEMENTED; }
 int gpe_energy_dipolar(double*, double*) { return GPE_ERR_NOT_IMPLEMENTED; }

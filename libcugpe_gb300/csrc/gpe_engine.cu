@@ -61,6 +61,60 @@ __global__ void k_set_state(DynState* d, unsigned it, double s_prev) {
 
 __global__ void k_reset_scale(DynState* d) { d->s_prev = 1.0; }
 
+// Phase enforcing, applied to psi (with the pending ITE scale) at the start of
+// a step.  mode 1: vortex line along z through (x0, y0), phase
+// Q atan2(x - x0, y - y0) (dev/gpe_engine.cu:485-511); mode 2: the same, only
+// where |psi| > 1e-15 (:520-548); mode 3: psi = |psi| exp(i phase[idx])
+// (:584-591).
+enum : int { ENF_VORTEX = 1, ENF_VORTEX2 = 2, ENF_PHASE = 3 };
+
+template <typename R>
+__global__ void k_enforce(C2<R>* psi, size_t n, const DynState* d, int mode, int ly, int lz, int nx, int ny,
+                          double x0, double y0, int q, const R* phase) {
+    const R s = (R)d->s_prev;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        C2<R> p = cscale(psi[i], s);
+        if (mode == ENF_PHASE) {
+            const R a = (R)sqrt(p.x * p.x + p.y * p.y);
+            R sn, cs;
+            gsincos(phase[i], &sn, &cs);
+            p.x = a * cs;
+            p.y = a * sn;
+        } else {
+            const int ix = (int)(i >> (ly + lz)), iy = (int)((i >> lz) & ((1u << ly) - 1));
+            const double xx = (double)ix - 1.0 * (nx / 2) - x0;
+            const double yy = (double)iy - 1.0 * (ny / 2) - y0;
+            const R a = (R)hypot((double)p.x, (double)p.y);
+            if (mode == ENF_VORTEX || a > (R)1e-15) {
+                const R ph = (R)(atan2(xx, yy) * (double)q);
+                R sn, cs;
+                gsincos(ph, &sn, &cs);
+                p.x = a * cs;
+                p.y = a * sn;
+            }
+        }
+        psi[i] = p;
+    }
+}
+
+template <typename R>
+__global__ void k_phase(const C2<R>* psi, R* phase, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        phase[i] = atan2(psi[i].y, psi[i].x);  // dev/gpe_engine.cu:552-559
+}
+
+template <typename R>
+__global__ void k_real_to_double(const R* in, double* out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = (double)in[i];
+}
+
+template <typename R>
+__global__ void k_real_from_double(const double* in, R* out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = (R)in[i];
+}
+
 template <typename R>
 __global__ void k_to_double(const C2<R>* in, double2* out, size_t n) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -152,6 +206,10 @@ struct Engine {
     double2* stage = nullptr;  // FP64 staging for host I/O of the FP32 form
     double* dens = nullptr;
     void* vextra = nullptr;
+    void* phase = nullptr;     // enforced phase field (R[n])
+    double vortex_x0 = 0.0, vortex_y0 = 0.0;
+    int vortex_q = 1;
+    bool vortex_set = false, phase_set = false;
     int vslices = 0, vsteps = 1;
 
     bool use_graph = true;
@@ -557,6 +615,45 @@ static int evolve(Engine* e, int nt, double* mu) {
     return cuda_rc(cudaGetLastError());
 }
 
+// gpe_evolve_vortex{,2,3} / gpe_evolve_enforced_phase (dev/gpe_engine.cu:1115-1477):
+// the enforcing op, then the regular step.  The reference repeats the op on
+// the unchanged psi in the middle of an ITE step (:1161, :1253, :1436); on an
+// already enforced psi that repeat changes nothing beyond rounding and is not
+// done here.  psi changes at every step start, so each step recomputes the
+// friction Laplacian and runs directly (no graph).
+template <typename R>
+static int enforce(Engine* e, int mode) {
+    int b, t;
+    util_grid(e->n, &b, &t);
+    k_enforce<R><<<b, t, 0, e->st>>>((C2<R>*)e->psi, e->n, e->dyn, mode, e->l3[1], e->l3[2], e->n3[0], e->n3[1],
+                                     e->vortex_x0, e->vortex_y0, e->vortex_q, (const R*)e->phase);
+    k_reset_scale<<<1, 1, 0, e->st>>>(e->dyn);
+    e->launches += 2;
+    return cuda_rc(cudaGetLastError());
+}
+
+static int evolve_enforced(Engine* e, int nt, double* mu, int mode) {
+    if (nt <= 0) return 0;
+    const std::vector<PassDesc> s = schedule(e, true);
+    e->passes_per_step = (int)s.size();
+    for (int i = 0; i < nt; i++) {
+        GPE_RC(e->prec == GPE_PRECISION_FP32 ? enforce<float>(e, mode) : enforce<double>(e, mode));
+        GPE_RC(run_steps(e, s, 1));
+    }
+    e->lap_valid = false;
+    if (e->beta != 0.0) {
+        GPE_RC(e->prec == GPE_PRECISION_FP32 ? finish_ite<float>(e) : finish_ite<double>(e));
+        if (mu) {
+            double m = 0.0;
+            GPE_CK(cudaMemcpyAsync(&m, &e->dyn->mu, sizeof(double), cudaMemcpyDeviceToHost, e->st));
+            GPE_CK(cudaStreamSynchronize(e->st));
+            *mu = m;
+        }
+    }
+    e->it += (unsigned)nt;
+    return cuda_rc(cudaGetLastError());
+}
+
 template <typename R>
 static int norm_to_slot(Engine* e, int slot) {
     k_norm<R><<<kRedBlocks, kRedThreads, 0, e->st>>>((const C2<R>*)e->psi, e->n, e->gamma, e->partials, e->dyn, slot);
@@ -617,6 +714,7 @@ static void release(Engine* e) {
     cudaFree(e->psi); cudaFree(e->psi2); cudaFree(e->lap); cudaFree(e->aux); cudaFree(e->V); cudaFree(e->Vqf);
     cudaFree(e->dyn); cudaFree(e->partials); cudaFree(e->tabmem); cudaFree(e->stage); cudaFree(e->dens);
     cudaFree(e->vextra);
+    cudaFree(e->phase);
     if (e->st) cudaStreamDestroy(e->st);
 }
 
@@ -890,6 +988,80 @@ int gpe_gb_set_potential_slices(gpe_gb_engine* h, const double* fields, int nsli
     e->vslices = nslices;
     e->vsteps = steps_per_slice;
     return 0;
+}
+
+int gpe_gb_set_vortex(gpe_gb_engine* h, double x0, double y0, int q) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    h->e.vortex_x0 = x0;
+    h->e.vortex_y0 = y0;
+    h->e.vortex_q = q;
+    h->e.vortex_set = true;
+    return 0;
+}
+
+static int phase_alloc(Engine* e) {
+    if (!e->phase) GPE_CK(cudaMalloc(&e->phase, e->rsize() * e->n));
+    if (!e->dens) GPE_CK(cudaMalloc(&e->dens, sizeof(double) * e->n));
+    return 0;
+}
+
+int gpe_gb_get_phase(gpe_gb_engine* h, double* phase) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    Engine* e = &h->e;
+    GPE_RC(phase_alloc(e));
+    int b, t;
+    gpe::util_grid(e->n, &b, &t);
+    if (e->prec == GPE_PRECISION_FP32) gpe::k_phase<float><<<b, t, 0, e->st>>>((const float2*)e->psi, (float*)e->phase, e->n);
+    else gpe::k_phase<double><<<b, t, 0, e->st>>>((const double2*)e->psi, (double*)e->phase, e->n);
+    e->launches++;
+    GPE_CK(cudaGetLastError());
+    e->phase_set = true;
+    if (phase) {
+        if (e->prec == GPE_PRECISION_FP32) {
+            gpe::k_real_to_double<float><<<b, t, 0, e->st>>>((const float*)e->phase, e->dens, e->n);
+            e->launches++;
+            GPE_CK(cudaMemcpyAsync(phase, e->dens, sizeof(double) * e->n, cudaMemcpyDeviceToHost, e->st));
+        } else {
+            GPE_CK(cudaMemcpyAsync(phase, e->phase, sizeof(double) * e->n, cudaMemcpyDeviceToHost, e->st));
+        }
+    }
+    return gpe::cuda_rc(cudaStreamSynchronize(e->st));
+}
+
+int gpe_gb_set_phase(gpe_gb_engine* h, const double* phase) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    if (!phase) return GPE_ERR_ARGUMENT;
+    Engine* e = &h->e;
+    GPE_RC(phase_alloc(e));
+    if (e->prec == GPE_PRECISION_FP32) {
+        GPE_CK(cudaMemcpyAsync(e->dens, phase, sizeof(double) * e->n, cudaMemcpyHostToDevice, e->st));
+        int b, t;
+        gpe::util_grid(e->n, &b, &t);
+        gpe::k_real_from_double<float><<<b, t, 0, e->st>>>(e->dens, (float*)e->phase, e->n);
+        e->launches++;
+        GPE_CK(cudaGetLastError());
+    } else {
+        GPE_CK(cudaMemcpyAsync(e->phase, phase, sizeof(double) * e->n, cudaMemcpyHostToDevice, e->st));
+    }
+    e->phase_set = true;
+    return gpe::cuda_rc(cudaStreamSynchronize(e->st));
+}
+
+int gpe_gb_evolve_vortex(gpe_gb_engine* h, int nt, double* mu, int method) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    if (method < 1 || method > 3) return GPE_ERR_ARGUMENT;
+    Engine* e = &h->e;
+    // methods 1 and 3 differ only in the mid-step repeat, which is not needed (see evolve_enforced)
+    GPE_RC(gpe::evolve_enforced(e, nt, mu, method == 2 ? gpe::ENF_VORTEX2 : gpe::ENF_VORTEX));
+    return gpe::cuda_rc(cudaStreamSynchronize(e->st));
+}
+
+int gpe_gb_evolve_enforced_phase(gpe_gb_engine* h, int nt, double* mu) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    Engine* e = &h->e;
+    if (!e->phase_set) return GPE_ERR_ARGUMENT;
+    GPE_RC(gpe::evolve_enforced(e, nt, mu, gpe::ENF_PHASE));
+    return gpe::cuda_rc(cudaStreamSynchronize(e->st));
 }
 
 const char* gpe_gb_error_string(int code) {

@@ -71,6 +71,11 @@ def lib():
         L.oracle_energy.argtypes = [vp, dp, dp, dp, dp]
         L.oracle_energy.restype = i
         L.oracle_fft3d.argtypes = [i, i, i, dp, i, i]
+        L.oracle_set_vortex.argtypes = [vp, d, d, i]
+        L.oracle_get_phase.argtypes = [vp, dp]
+        L.oracle_set_phase.argtypes = [vp, dp]
+        L.oracle_evolve_enforced.argtypes = [vp, i, dp, i]
+        L.oracle_evolve_enforced.restype = i
         _lib = L
     return _lib
 
@@ -144,6 +149,28 @@ class Oracle:
     def evolve_qf(self, nt):
         mu = ctypes.c_double(0.0)
         lib().oracle_evolve_qf(self._h, int(nt), ctypes.byref(mu))
+        return mu.value
+
+    def set_vortex(self, x0, y0, q=1):
+        lib().oracle_set_vortex(self._h, float(x0), float(y0), int(q))
+
+    def get_phase(self):
+        out = np.empty(self.shape, dtype=np.float64)
+        lib().oracle_get_phase(self._h, _dp(out))
+        return out
+
+    def set_phase(self, phase):
+        p = np.ascontiguousarray(phase, dtype=np.float64).reshape(self.shape)
+        lib().oracle_set_phase(self._h, _dp(p))
+
+    def evolve_vortex(self, nt, method=1):
+        mu = ctypes.c_double(0.0)
+        lib().oracle_evolve_enforced(self._h, int(nt), ctypes.byref(mu), int(method))
+        return mu.value
+
+    def evolve_enforced_phase(self, nt):
+        mu = ctypes.c_double(0.0)
+        lib().oracle_evolve_enforced(self._h, int(nt), ctypes.byref(mu), 4)
         return mu.value
 
     def energy(self):

@@ -65,6 +65,10 @@ typedef struct {
     /* optional additive potential: nslices fields of n doubles */
     const double *vextra;
     int nslices, steps_per_slice;
+    /* phase enforcing (dev/gpe_engine.cu:465-591) */
+    double vx0, vy0;
+    int vq;
+    double *phase;
 } gpe_oracle;
 
 /* ---------------------------------------------------------------- helpers */
@@ -277,6 +281,7 @@ void oracle_destroy(void *h) {
     free(o->kx); free(o->ky); free(o->kz); free(o->ex); free(o->ey); free(o->ez);
     for (int a = 0; a < 3; a++) free(o->tw[a]);
     free(o->psi); free(o->psi2); free(o->wrkC); free(o->wrk3C); free(o->V); free(o->Vqf); free(o->rho);
+    free(o->phase);
     free(o);
 }
 
@@ -395,13 +400,69 @@ static void qf_potential(gpe_oracle *o, const cd *psi) {
     }
 }
 
-int oracle_evolve_qf(void *h, int nt, double *mu) {
+/* enforcing ops: 1 vortex imprint (dev/gpe_engine.cu:485-511), 2 imprint
+ * where |psi| > 1e-15 (:520-548), 3 psi = |psi| exp(i phase) (:584-591) */
+static void enforce(gpe_oracle *o, int mode) {
+    const int ny = o->ny, nz = o->nz;
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+    for (long i = 0; i < (long)o->n; i++) {
+        DECODE((size_t)i);
+        (void)iz;
+        cd p = o->psi[i];
+        if (mode == 3) {
+            const double a = sqrt(p.x * p.x + p.y * p.y);
+            p.x = a * cos(o->phase[i]);
+            p.y = a * sin(o->phase[i]);
+        } else {
+            const double xx = (double)ix - 1.0 * (o->nx / 2) - o->vx0;
+            const double yy = (double)iy - 1.0 * (o->ny / 2) - o->vy0;
+            const double a = hypot(p.x, p.y);
+            if (mode == 1 || a > 1e-15) {
+                const double ph = atan2(xx, yy) * (double)o->vq;
+                p.x = a * cos(ph);
+                p.y = a * sin(ph);
+            }
+        }
+        o->psi[i] = p;
+    }
+}
+
+void oracle_set_vortex(void *h, double x0, double y0, int q) {
     gpe_oracle *o = (gpe_oracle *)h;
+    o->vx0 = x0; o->vy0 = y0; o->vq = q;
+}
+
+void oracle_get_phase(void *h, double *out) {
+    gpe_oracle *o = (gpe_oracle *)h;
+    if (!o->phase) o->phase = malloc(sizeof(double) * o->n);
+    for (size_t i = 0; i < o->n; i++) o->phase[i] = atan2(o->psi[i].y, o->psi[i].x);
+    if (out) memcpy(out, o->phase, sizeof(double) * o->n);
+}
+
+void oracle_set_phase(void *h, const double *ph) {
+    gpe_oracle *o = (gpe_oracle *)h;
+    if (!o->phase) o->phase = malloc(sizeof(double) * o->n);
+    memcpy(o->phase, ph, sizeof(double) * o->n);
+}
+
+static int evolve_impl(gpe_oracle *o, int nt, double *mu, int mode, int mid_repeat);
+
+int oracle_evolve_qf(void *h, int nt, double *mu) { return evolve_impl((gpe_oracle *)h, nt, mu, 0, 0); }
+
+/* gpe_evolve_vortex{,2,3} and gpe_evolve_enforced_phase (dev/gpe_engine.cu:1115-1477):
+ * kind 1, 2, 3 vortex methods, 4 enforced phase */
+int oracle_evolve_enforced(void *h, int nt, double *mu, int kind) {
+    const int mode = (kind == 2) ? 2 : (kind == 4) ? 3 : 1;
+    return evolve_impl((gpe_oracle *)h, nt, mu, mode, kind != 3);
+}
+
+static int evolve_impl(gpe_oracle *o, int nt, double *mu, int mode, int mid_repeat) {
     const int ny = o->ny, nz = o->nz;
     const long n = (long)o->n;
     const int qf = o->qfcoeff != 0.0;
     for (int step = 0; step < nt; step++) {
         const unsigned it = o->it;
+        if (mode) enforce(o, mode);
         /* Vstep1 / Vstep1_qf: dev/gpe_engine.cu:719-768, 1038-1047 */
         if (qf) qf_potential(o, o->psi);
 #pragma omp parallel for num_threads(o->nthreads) schedule(static)
@@ -435,7 +496,10 @@ int oracle_evolve_qf(void *h, int nt, double *mu) {
             /* part1: dev/gpe_engine.cu:799-811 */
 #pragma omp parallel for num_threads(o->nthreads) schedule(static)
             for (long i = 0; i < n; i++) o->psi2[i] = cmul(o->psi2[i], cexp_(cscale(o->c3, o->V[i])));
-            if (o->beta != 0.0) normalize(o, o->psi2);
+            if (o->beta != 0.0) {
+                normalize(o, o->psi2);
+                if (mode && mid_repeat) enforce(o, mode); /* :1161, :1253, :1436 */
+            }
             if (qf) qf_potential(o, o->psi);
             /* part2 / part2_qf: dev/gpe_engine.cu:813-864 */
 #pragma omp parallel for num_threads(o->nthreads) schedule(static)

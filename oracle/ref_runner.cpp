@@ -17,6 +17,10 @@
 //     D      gpe_get_psi() -> OUTDIR/psi_<i>.bin
 //     R / I  gpe_set_rte_evolution() / gpe_set_ite_evolution()
 //     Q<x>   gpe_set_quantum_friction_coeff(x)
+//     X<x0>/<y0>/<q>  gpe_set_vortex(x0, y0, q)
+//     V<m>_<k>  gpe_evolve_vortex (m=1), _vortex2 (2), _vortex3 (3), k steps -> "MU mu"
+//     G      gpe_get_phase(NULL)
+//     P<k>   gpe_evolve_enforced_phase(k, &mu) -> "MU mu"
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -92,6 +96,25 @@ int main(int argc, char** argv) {
             CHECK(gpe_set_ite_evolution());
         } else if (c[0] == 'Q') {
             CHECK(gpe_set_quantum_friction_coeff(atof(c.c_str() + 1)));
+        } else if (c[0] == 'X') {
+            double x0 = 0, y0 = 0;
+            int q = 1;
+            sscanf(c.c_str() + 1, "%lf/%lf/%d", &x0, &y0, &q);
+            CHECK(gpe_set_vortex(x0, y0, (int8_t)q));
+        } else if (c[0] == 'V') {
+            int m = 1, k = 0;
+            sscanf(c.c_str() + 1, "%d_%d", &m, &k);
+            double mu = 0.0;
+            if (m == 1) CHECK(gpe_evolve_vortex(k, &mu));
+            else if (m == 2) CHECK(gpe_evolve_vortex2(k, &mu));
+            else CHECK(gpe_evolve_vortex3(k, &mu));
+            printf("MU %.17g\n", mu);
+        } else if (c == "G") {
+            CHECK(gpe_get_phase(NULL));
+        } else if (c[0] == 'P') {
+            double mu = 0.0;
+            CHECK(gpe_evolve_enforced_phase(atoi(c.c_str() + 1), &mu));
+            printf("MU %.17g\n", mu);
         } else {
             fprintf(stderr, "unknown command %s\n", c.c_str());
             return 1;

@@ -173,3 +173,25 @@ def test_time_sliced_potential_matches_oracle(cuda_device, gpe_lib):
     en_e, en_o = e.energy(), o.energy()
     for a, b in zip(en_e[1:], en_o[1:]):
         assert abs(a - b) <= 1e-10 * max(1.0, abs(b))
+
+
+@pytest.mark.parametrize("case", ["bec_ite", "ufg_ite_qf", "bec_rte", "ufg_rte_qf"])
+@pytest.mark.parametrize("method", [1, 2, 3, 4])
+def test_phase_enforcing_evolves_match_oracle(cuda_device, gpe_lib, case, method):
+    """gpe_evolve_vortex{,2,3} (methods 1-3) and gpe_evolve_enforced_phase (4)."""
+    shape = (16, 16, 16)
+    e, o, psi = make_pair(shape, case)
+    if method == 4:
+        rng = np.random.default_rng(5)
+        ph = rng.uniform(-np.pi, np.pi, shape)
+        e.set_phase(ph)
+        o.set_phase(ph)
+        mu_e, mu_o = e.evolve_enforced_phase(3), o.evolve_enforced_phase(3)
+    else:
+        e.set_vortex(0.5, -0.5, 1)
+        o.set_vortex(0.5, -0.5, 1)
+        mu_e, mu_o = e.evolve_vortex(3, method), o.evolve_vortex(3, method)
+    assert rel(e.get_psi()[1], o.get_psi()[1]) <= 3e-12
+    if CASES[case][2] != 0.0:
+        assert abs(mu_e - mu_o) <= 1e-10 * max(1.0, abs(mu_o))
+    np.testing.assert_allclose(e.get_phase(), o.get_phase(), atol=1e-9)

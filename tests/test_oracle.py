@@ -149,3 +149,21 @@ def test_oracle_matches_reference_golden_vectors(path):
     t, ek, ei, ee = o.energy()
     for a, b in zip((ek, ei, ee), meta["energy"]):
         assert abs(a - b) < 1e-10 * max(1.0, abs(b))
+
+
+def test_vortex_imprint_keeps_winding_through_ite():
+    """ITE with the vortex enforced (gpe_evolve_vortex) keeps a 2*pi winding around (x0, y0)."""
+    shape = (16, 16, 8)
+    o = oracle.Oracle(shape, -1, 0.0, 1.0, 0.05, 1.0, threads=2)
+    o.set_user_params([0.1, 0.1, 0.1, 1.0])
+    o.set_psi(0.0, configs.random_state(shape, seed=8, phase=False))
+    o.set_vortex(0.5, 0.5, 1)
+    o.evolve_vortex(10, 1)
+    ph = o.get_phase()[:, :, 4]
+    # walk a square loop around the line through the box centre + (0.5, 0.5)
+    loop = [(6, j) for j in range(6, 11)] + [(i, 10) for i in range(7, 11)] + \
+           [(10, j) for j in range(9, 5, -1)] + [(i, 6) for i in range(9, 5, -1)]
+    w = 0.0
+    for (a, b), (c, d) in zip(loop, loop[1:] + loop[:1]):
+        w += (ph[c, d] - ph[a, b] + np.pi) % (2 * np.pi) - np.pi
+    assert abs(abs(w) - 2 * np.pi) < 1e-6

@@ -106,3 +106,25 @@ def test_bec_64_ite_matches_reference(reference, gpe_lib):
     assert abs(mu - out["mu"][0]) <= 1e-9 * abs(out["mu"][0])
     etot, etot_ref = sum(en[1:]), sum(out["energy"][0][1:])
     assert abs(etot - etot_ref) <= 1e-11 * abs(etot_ref)
+
+
+@pytest.mark.parametrize("beta", [1.0, 0.0])
+@pytest.mark.parametrize("method", [1, 2, 3, "P"])
+def test_phase_enforcing_evolves_match_reference(reference, gpe_lib, beta, method):
+    shape, inter, npart, params, qf = (16, 16, 16), -1, 1.0, [0.0625, 0.0625, 0.0625, 31.83], 0.0
+    alpha = 1.0 - beta
+    psi = configs.random_state(shape, seed=23, npart=npart)
+    e = engine_for(shape, inter, alpha, beta, 0.05, npart, params, qf, psi)
+    if method == "P":
+        cmds = ["G", "P4", "D"]
+        e.get_phase()
+        mu = e.evolve_enforced_phase(4)
+    else:
+        cmds = ["X0.5/-0.5/1", f"V{method}_4", "D"]
+        e.set_vortex(0.5, -0.5, 1)
+        mu = e.evolve_vortex(4, method)
+    out = ref_run.run(shape, inter, alpha, beta, 0.05, npart, params, psi, cmds, qf=qf)
+    _, ours = e.get_psi()
+    assert rel(ours, out["psi"][0]) <= 3e-12, rel(ours, out["psi"][0])
+    if beta != 0.0:
+        assert abs(mu - out["mu"][0]) <= 1e-10 * max(1.0, abs(out["mu"][0]))
