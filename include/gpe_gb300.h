@@ -93,6 +93,9 @@ int gpe_gb_get_psi_device(gpe_gb_engine* e, double* t, void* psi);
 /* The CUDA stream (cudaStream_t) this engine launches on, for callers that
  * order their own work or events against it. */
 void* gpe_gb_get_stream(const gpe_gb_engine* e);
+/* mu of the last ITE step and its change over that step (the reference
+ * returns mu through gpe_evolve_qf only; this also serves convergence tests). */
+int gpe_gb_chemical_potential(gpe_gb_engine* e, double* mu, double* dmu);
 /* Runs all queued work to completion. */
 int gpe_gb_synchronize(gpe_gb_engine* e);
 /* Number of kernels this engine has launched so far. */
@@ -127,6 +130,27 @@ int gpe_gb_set_potential_slices(gpe_gb_engine* e, const double* fields, int nsli
  * overlap on the GPU (different streams, or host threads) race and must be
  * serialised by the caller. */
 int gpe_gb_norm_noalloc(const void* psi, int precision, long long n, double gamma, double* norm_out, void* stream);
+/* Batched solver (no reference counterpart; the reference runs one
+ * condensate per process).  `count` independent condensates, condensate i on
+ * a sides[3i] x sides[3i+1] x sides[3i+2] lattice (each side 32, 64, 128 or
+ * 256) with its own time step dt[i] and npart[i]; common functional, alpha,
+ * beta; FP32-mixed only.  Every fused pass of a step is one launch over all active
+ * condensates, whatever their sizes, and runs of steps replay from one
+ * captured CUDA graph.  Per-condensate parameters, psi and observables go
+ * through the condensate's engine handle (gpe_gb_batch_engine); quantum
+ * friction is not supported in a batch. */
+typedef struct gpe_gb_batch gpe_gb_batch;
+int gpe_gb_batch_create(gpe_gb_batch** out, int count, const int* sides, int interactions, int precision,
+                        double alpha, double beta, const double* dt, const double* npart);
+int gpe_gb_batch_destroy(gpe_gb_batch* b);
+gpe_gb_engine* gpe_gb_batch_engine(gpe_gb_batch* b, int i);
+/* Inactive condensates are skipped (e.g. once converged). */
+int gpe_gb_batch_set_active(gpe_gb_batch* b, int i, int active);
+/* nt steps of every active condensate (gpe_evolve_qf semantics per condensate). */
+int gpe_gb_batch_evolve(gpe_gb_batch* b, int nt);
+/* Per condensate: mu of the last step and its change over that step (ITE). */
+int gpe_gb_batch_chemical_potentials(gpe_gb_batch* b, double* mu, double* dmu);
+long long gpe_gb_batch_kernel_launches(const gpe_gb_batch* b);
 /* Message for a return code. */
 const char* gpe_gb_error_string(int code);
 

@@ -43,7 +43,9 @@ C_ABI_SYMBOLS = [
     "gpe_gb_set_psi_device", "gpe_gb_get_psi_device", "gpe_gb_synchronize", "gpe_gb_kernel_launches",
     "gpe_gb_use_graphs", "gpe_gb_set_potential_slices", "gpe_gb_error_string", "gpe_gb_get_stream",
     "gpe_gb_profile_passes", "gpe_gb_norm_noalloc", "gpe_gb_set_vortex", "gpe_gb_get_phase", "gpe_gb_set_phase",
-    "gpe_gb_evolve_vortex", "gpe_gb_evolve_enforced_phase",
+    "gpe_gb_evolve_vortex", "gpe_gb_evolve_enforced_phase", "gpe_gb_batch_create", "gpe_gb_batch_destroy",
+    "gpe_gb_batch_engine", "gpe_gb_batch_set_active", "gpe_gb_batch_evolve", "gpe_gb_batch_chemical_potentials",
+    "gpe_gb_batch_kernel_launches", "gpe_gb_chemical_potential",
 ]
 
 
@@ -95,6 +97,14 @@ def _lib():
             "gpe_gb_set_phase": (i, [vp, dp]),
             "gpe_gb_evolve_vortex": (i, [vp, i, dp, i]),
             "gpe_gb_evolve_enforced_phase": (i, [vp, i, dp]),
+            "gpe_gb_batch_create": (i, [ctypes.POINTER(vp), i, ip, i, i, d, d, dp, dp]),
+            "gpe_gb_batch_destroy": (i, [vp]),
+            "gpe_gb_batch_engine": (vp, [vp, i]),
+            "gpe_gb_batch_set_active": (i, [vp, i, i]),
+            "gpe_gb_batch_evolve": (i, [vp, i]),
+            "gpe_gb_batch_chemical_potentials": (i, [vp, dp, dp]),
+            "gpe_gb_batch_kernel_launches": (ctypes.c_longlong, [vp]),
+            "gpe_gb_chemical_potential": (i, [vp, dp, dp]),
             "gpe_gb_profile_passes": (i, [vp, i, ctypes.POINTER(ctypes.c_float), dp, ip, ip, i, ip]),
         }
         for name, (res, args) in sig.items():
@@ -121,10 +131,15 @@ def _check(rc: int, where: str):
 class Engine:
     """One condensate on the GPU; the methods follow the reference API."""
 
-    def __init__(self, shape, interactions=-1, alpha=0.0, beta=1.0, dt=1e-3, npart=1.0, precision=FP64):
+    def __init__(self, shape, interactions=-1, alpha=0.0, beta=1.0, dt=1e-3, npart=1.0, precision=FP64,
+                 _handle=None):
         self.shape = tuple(int(s) for s in shape)
         self.precision = precision
         self.alpha, self.beta, self.dt, self.npart = alpha, beta, dt, npart
+        self._owned = _handle is None
+        if _handle is not None:  # a condensate owned by a Batch
+            self._h = ctypes.c_void_p(_handle)
+            return
         L = _lib()
         h = ctypes.c_void_p()
         _check(L.gpe_gb_create(ctypes.byref(h), *self.shape, int(interactions), int(precision),
@@ -132,9 +147,9 @@ class Engine:
         self._h = h
 
     def close(self):
-        if getattr(self, "_h", None):
+        if getattr(self, "_h", None) and self._owned:
             _lib().gpe_gb_destroy(self._h)
-            self._h = None
+        self._h = None
 
     def __del__(self):
         try:
@@ -225,6 +240,12 @@ class Engine:
         _check(_lib().gpe_gb_evolve_enforced_phase(self._h, int(nt), ctypes.byref(mu)), "evolve_enforced_phase")
         return mu.value
 
+    def chemical_potential(self):
+        """(mu, change of mu) of the last ITE step."""
+        mu, dmu = ctypes.c_double(), ctypes.c_double()
+        _check(_lib().gpe_gb_chemical_potential(self._h, ctypes.byref(mu), ctypes.byref(dmu)), "chemical_potential")
+        return mu.value, dmu.value
+
     def energy(self):
         t, a, b, c = (ctypes.c_double() for _ in range(4))
         _check(_lib().gpe_gb_energy(self._h, ctypes.byref(t), ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
@@ -264,3 +285,56 @@ class Engine:
         self._slices = f
         _check(_lib().gpe_gb_set_potential_slices(self._h, _dp(f), f.shape[0], int(steps_per_slice)),
                "set_potential_slices")
+
+
+class Batch:
+    """Independent condensates stepped together (FP32-mixed): one launch per
+    fused pass covers every active condensate, whatever its lattice size."""
+
+    def __init__(self, shapes, interactions=-1, alpha=0.0, beta=1.0, dt=1e-3, npart=None, precision=FP32):
+        L = _lib()
+        shapes = [tuple(int(x) for x in s) for s in shapes]
+        n = len(shapes)
+        npart = [1.0] * n if npart is None else list(npart)
+        dts = [float(dt)] * n if np.isscalar(dt) else [float(x) for x in dt]
+        sides = (ctypes.c_int * (3 * n))(*[x for s in shapes for x in s])
+        nps = (ctypes.c_double * n)(*[float(x) for x in npart])
+        dtp = (ctypes.c_double * n)(*dts)
+        h = ctypes.c_void_p()
+        _check(L.gpe_gb_batch_create(ctypes.byref(h), n, sides, int(interactions), int(precision), float(alpha),
+                                     float(beta), dtp, nps), "gpe_gb_batch_create")
+        self._h = h
+        self.engines = [Engine(shapes[i], interactions, alpha, beta, dts[i], npart[i], precision,
+                               _handle=L.gpe_gb_batch_engine(h, i)) for i in range(n)]
+
+    def __len__(self):
+        return len(self.engines)
+
+    def evolve(self, nt):
+        _check(_lib().gpe_gb_batch_evolve(self._h, int(nt)), "batch_evolve")
+
+    def set_active(self, i, active):
+        _check(_lib().gpe_gb_batch_set_active(self._h, int(i), 1 if active else 0), "batch_set_active")
+
+    def chemical_potentials(self):
+        n = len(self.engines)
+        mu = np.zeros(n)
+        dmu = np.zeros(n)
+        _check(_lib().gpe_gb_batch_chemical_potentials(self._h, _dp(mu), _dp(dmu)), "batch_chemical_potentials")
+        return mu, dmu
+
+    def kernel_launches(self) -> int:
+        return int(_lib().gpe_gb_batch_kernel_launches(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            for e in self.engines:
+                e._h = None
+            _lib().gpe_gb_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,48 @@
+// Instantiation of the batched pass kernels (FP32-mixed form) and their
+// launch dispatch over (axis, kernel class).
+#include "gpe_batch.cuh"
+
+namespace gpe {
+
+template <typename R, int AX, int CLS>
+static cudaError_t launch_b(const BatchItem<R>* items, int nitems, unsigned grid, size_t smem, cudaStream_t st) {
+    static bool configured = false;  // single device
+    if (!configured) {
+        size_t mx = PassGeom<R, 32, AX, kBatchThreads>::SMEM_MAX;
+        if (PassGeom<R, 64, AX, kBatchThreads>::SMEM_MAX > mx) mx = PassGeom<R, 64, AX, kBatchThreads>::SMEM_MAX;
+        if (PassGeom<R, 128, AX, kBatchThreads>::SMEM_MAX > mx) mx = PassGeom<R, 128, AX, kBatchThreads>::SMEM_MAX;
+        if (PassGeom<R, 256, AX, kBatchThreads>::SMEM_MAX > mx) mx = PassGeom<R, 256, AX, kBatchThreads>::SMEM_MAX;
+        cudaError_t e = cudaFuncSetAttribute(pass_batch_kernel<R, AX, CLS>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx);
+        if (e != cudaSuccess) return e;
+        e = cudaFuncSetAttribute(pass_batch_kernel<R, AX, CLS>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    pass_batch_kernel<R, AX, CLS><<<grid, kBatchThreads, smem, st>>>(items, nitems);
+    return cudaGetLastError();
+}
+
+template <typename R, int AX>
+static cudaError_t launch_bc(int cls, const BatchItem<R>* items, int nitems, unsigned grid, size_t smem,
+                             cudaStream_t st) {
+    switch (cls) {
+        case C_KIN: return launch_b<R, AX, C_KIN>(items, nitems, grid, smem, st);
+        case C_EPI: return launch_b<R, AX, C_EPI>(items, nitems, grid, smem, st);
+        case C_LAP: return launch_b<R, AX, C_LAP>(items, nitems, grid, smem, st);
+        default: return launch_b<R, AX, C_EN>(items, nitems, grid, smem, st);
+    }
+}
+
+template <>
+cudaError_t launch_batch<float>(int axis, int cls, const BatchItem<float>* items, int nitems, unsigned grid,
+                                size_t smem, cudaStream_t st) {
+    switch (axis) {
+        case AX_X: return launch_bc<float, AX_X>(cls, items, nitems, grid, smem, st);
+        case AX_Y: return launch_bc<float, AX_Y>(cls, items, nitems, grid, smem, st);
+        default: return launch_bc<float, AX_Z>(cls, items, nitems, grid, smem, st);
+    }
+}
+
+}  // namespace gpe

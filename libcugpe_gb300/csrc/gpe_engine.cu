@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "gpe_launch.cuh"
+#include "gpe_batch.cuh"
 #include "../../include/gpe_gb300.h"
 
 namespace gpe {
@@ -214,6 +215,7 @@ struct Engine {
 
     bool use_graph = true;
     bool graph_dirty = true;
+    unsigned version = 0;  // bumped whenever tables or captured arguments change
     bool lap_valid = false;  // lap holds the z-Laplacian term of the current psi
     cudaGraphExec_t gexec = nullptr;
     int gsteps = 0;
@@ -332,6 +334,7 @@ static int upload_tables(Engine* e) {
     GPE_CK(cudaMemcpyAsync(e->tabmem, host.data(), off, cudaMemcpyHostToDevice, e->st));
     GPE_CK(cudaStreamSynchronize(e->st));
     e->graph_dirty = true;
+    e->version++;
     return 0;
 }
 
@@ -445,7 +448,7 @@ static void axis_args(const Engine* e, PassArgs<R>& a, int axis) {
 static size_t pencils_of(const Engine* e, int axis) { return e->n / (size_t)e->n3[axis]; }
 
 template <typename R>
-static int launch_desc(Engine* e, const PassDesc& d) {
+static PassArgs<R> desc_args(const Engine* e, const PassDesc& d) {
     PassArgs<R> a = base_args<R>(e);
     axis_args(e, a, d.axis);
     a.ltab = (const R*)e->ax[d.axis].lqf;
@@ -453,6 +456,13 @@ static int launch_desc(Engine* e, const PassDesc& d) {
     a.out = (C2<R>*)(d.out == B_PSI ? e->psi : d.out == B_PSI2 ? e->psi2 : nullptr);
     a.pre = d.pre; a.mid = d.mid; a.post = d.post;
     a.flags = d.flags | (e->vextra ? F_VEXTRA : 0u);
+    a.npencils = (uint32_t)pencils_of(e, d.axis);
+    return a;
+}
+
+template <typename R>
+static int launch_desc(Engine* e, const PassDesc& d) {
+    const PassArgs<R> a = desc_args<R>(e, d);
     e->launches++;
     return cuda_rc(launch_pass<R>(a, e->n3[d.axis], d.axis, pencils_of(e, d.axis), e->st));
 }
@@ -730,6 +740,149 @@ struct gpe_gb_engine {
     Engine e;
 };
 
+// A batch of independent condensates stepped together: every fused pass of a
+// step is one launch over all active condensates (gpe_batch.cuh), and a run of
+// steps is replayed from one captured CUDA graph.
+struct gpe_gb_batch {
+    std::vector<gpe_gb_engine*> eng;
+    std::vector<char> active;
+    std::vector<unsigned> built_version;
+    cudaStream_t st = nullptr;
+    struct Launch {
+        void* items = nullptr;
+        int nitems = 0, axis = 0, cls = 0;
+        unsigned grid = 0;
+        size_t smem = 0;
+    };
+    std::vector<Launch> passes;
+    bool dirty = true;
+    cudaGraphExec_t gexec = nullptr;
+    int gsteps = 0;
+    long long launches = 0;
+};
+
+namespace gpe {
+
+static void batch_free_items(gpe_gb_batch* b) {
+    for (auto& l : b->passes) cudaFree(l.items);
+    b->passes.clear();
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    b->gexec = nullptr;
+    b->gsteps = 0;
+}
+
+template <int AX>
+static bool batch_shape_axis(int n, size_t pencils, uint32_t ops, uint32_t* nctas, size_t* smem) {
+    return batch_shape<float, AX>(n, pencils, ops, nctas, smem);
+}
+
+static int batch_build(gpe_gb_batch* b) {
+    batch_free_items(b);
+    int first = -1;
+    for (size_t i = 0; i < b->eng.size(); i++)
+        if (b->active[i]) { first = (int)i; break; }
+    if (first < 0) { b->dirty = false; return 0; }
+    const std::vector<PassDesc> s = schedule(&b->eng[first]->e, false);
+    for (const PassDesc& d : s) {
+        std::vector<BatchItem<float>> items;
+        size_t smem = 0;
+        uint32_t cta = 0;
+        for (size_t i = 0; i < b->eng.size(); i++) {
+            if (!b->active[i]) continue;
+            const Engine* e = &b->eng[i]->e;
+            BatchItem<float> it;
+            memset(&it, 0, sizeof it);
+            it.a = desc_args<float>(e, d);
+            it.n = e->n3[d.axis];
+            uint32_t nctas = 0;
+            size_t sm = 0;
+            const uint32_t ops = staged_ops(d.mid, d.post, it.a.flags);
+            const bool ok = (d.axis == AX_X) ? batch_shape_axis<AX_X>(it.n, it.a.npencils, ops, &nctas, &sm)
+                          : (d.axis == AX_Y) ? batch_shape_axis<AX_Y>(it.n, it.a.npencils, ops, &nctas, &sm)
+                                             : batch_shape_axis<AX_Z>(it.n, it.a.npencils, ops, &nctas, &sm);
+            if (!ok) return GPE_ERR_LATTICE;
+            it.cta_begin = cta;
+            it.nctas = nctas;
+            cta += nctas;
+            if (sm > smem) smem = sm;
+            items.push_back(it);
+        }
+        gpe_gb_batch::Launch l;
+        l.nitems = (int)items.size();
+        l.axis = d.axis;
+        l.cls = op_class(d.pre, d.mid, d.post, items[0].a.flags);
+        l.grid = cta;
+        l.smem = smem;
+        GPE_CK(cudaMalloc(&l.items, sizeof(BatchItem<float>) * items.size()));
+        GPE_CK(cudaMemcpy(l.items, items.data(), sizeof(BatchItem<float>) * items.size(), cudaMemcpyHostToDevice));
+        b->passes.push_back(l);
+    }
+    for (size_t i = 0; i < b->eng.size(); i++) b->built_version[i] = b->eng[i]->e.version;
+    b->dirty = false;
+    return 0;
+}
+
+static int batch_steps(gpe_gb_batch* b, int k) {
+    for (int i = 0; i < k; i++)
+        for (const auto& l : b->passes) {
+            GPE_CK(launch_batch<float>(l.axis, l.cls, (const BatchItem<float>*)l.items, l.nitems, l.grid, l.smem,
+                                       b->st));
+            b->launches++;
+        }
+    return 0;
+}
+
+static int batch_evolve(gpe_gb_batch* b, int nt) {
+    if (nt <= 0) return 0;
+    bool stale = b->dirty;
+    for (size_t i = 0; i < b->eng.size(); i++) {
+        Engine* e = &b->eng[i]->e;
+        if (!b->active[i]) continue;
+        if (e->qf_raw != 0.0 || e->prec != GPE_PRECISION_FP32) return GPE_ERR_ARGUMENT;
+        if (e->version != b->built_version[i]) stale = true;
+    }
+    if (stale) GPE_RC(batch_build(b));
+    if (b->passes.empty()) return 0;
+    int done = 0;
+    // one direct step first (configures the kernels outside capture), then graph replays
+    GPE_RC(batch_steps(b, 1));
+    done = 1;
+    const int chunk = 16;
+    if (nt - done >= chunk && b->gsteps != chunk) {
+        cudaGraph_t g = nullptr;
+        GPE_CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+        const long long before = b->launches;
+        const int rc = batch_steps(b, chunk);
+        b->launches = before;
+        cudaError_t ce = cudaStreamEndCapture(b->st, &g);
+        if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+        GPE_CK(ce);
+        if (b->gexec) cudaGraphExecDestroy(b->gexec);
+        ce = cudaGraphInstantiate(&b->gexec, g, 0);
+        cudaGraphDestroy(g);
+        GPE_CK(ce);
+        b->gsteps = chunk;
+    }
+    while (b->gexec && nt - done >= b->gsteps) {
+        GPE_CK(cudaGraphLaunch(b->gexec, b->st));
+        b->launches += (long long)b->gsteps * (long long)b->passes.size();
+        done += b->gsteps;
+    }
+    GPE_RC(batch_steps(b, nt - done));
+    GPE_CK(cudaStreamSynchronize(b->st));
+    for (size_t i = 0; i < b->eng.size(); i++) {
+        if (!b->active[i]) continue;
+        Engine* e = &b->eng[i]->e;
+        if (e->beta != 0.0) GPE_RC(finish_ite<float>(e));
+        e->it += (unsigned)nt;
+    }
+    for (size_t i = 0; i < b->eng.size(); i++)
+        if (b->active[i]) GPE_CK(cudaStreamSynchronize(b->eng[i]->e.st));
+    return 0;
+}
+
+}  // namespace gpe
+
 extern "C" {
 
 int gpe_gb_create(gpe_gb_engine** out, int nx, int ny, int nz, int interactions, int precision, double alpha,
@@ -944,6 +1097,17 @@ int gpe_gb_energy(gpe_gb_engine* h, double* t, double* ekin, double* eint, doubl
                                          : gpe::energy<double>(e, ekin, eint, eext);
 }
 
+int gpe_gb_chemical_potential(gpe_gb_engine* h, double* mu, double* dmu) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    if (!mu || !dmu) return GPE_ERR_ARGUMENT;
+    gpe::DynState d;
+    GPE_CK(cudaMemcpyAsync(&d, h->e.dyn, sizeof d, cudaMemcpyDeviceToHost, h->e.st));
+    GPE_CK(cudaStreamSynchronize(h->e.st));
+    *mu = d.mu;
+    *dmu = d.dmu;
+    return 0;
+}
+
 int gpe_gb_synchronize(gpe_gb_engine* h) {
     if (!h) return GPE_ERR_NO_ENGINE;
     return gpe::cuda_rc(cudaStreamSynchronize(h->e.st));
@@ -974,6 +1138,7 @@ int gpe_gb_set_potential_slices(gpe_gb_engine* h, const double* fields, int nsli
     e->vextra = nullptr;
     e->vslices = 0;
     e->graph_dirty = true;
+    e->version++;
     if (!fields) return 0;
     if (nslices <= 0 || steps_per_slice <= 0) return GPE_ERR_ARGUMENT;
     const size_t cnt = (size_t)nslices * e->n;
@@ -1063,6 +1228,82 @@ int gpe_gb_evolve_enforced_phase(gpe_gb_engine* h, int nt, double* mu) {
     GPE_RC(gpe::evolve_enforced(e, nt, mu, gpe::ENF_PHASE));
     return gpe::cuda_rc(cudaStreamSynchronize(e->st));
 }
+
+int gpe_gb_batch_create(gpe_gb_batch** out, int count, const int* sides, int interactions, int precision,
+                        double alpha, double beta, const double* dt, const double* npart) {
+    if (!out || !sides || !npart || !dt || count <= 0) return GPE_ERR_ARGUMENT;
+    *out = nullptr;
+    if (precision != GPE_PRECISION_FP32) return GPE_ERR_ARGUMENT;
+    for (int i = 0; i < 3 * count; i++) {
+        const int n = sides[i];
+        if (n != 32 && n != 64 && n != 128 && n != 256) return GPE_ERR_LATTICE;
+    }
+    gpe_gb_batch* b = new (std::nothrow) gpe_gb_batch();
+    if (!b) return GPE_ERR_ARGUMENT;
+    int rc = 0;
+    cudaError_t ce = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) rc = (int)ce;
+    for (int i = 0; i < count && !rc; i++) {
+        gpe_gb_engine* h = nullptr;
+        rc = gpe_gb_create(&h, sides[3 * i], sides[3 * i + 1], sides[3 * i + 2], interactions, precision, alpha, beta,
+                           dt[i], npart[i]);
+        if (!rc) b->eng.push_back(h);
+    }
+    if (rc) {
+        for (auto* h : b->eng) gpe_gb_destroy(h);
+        if (b->st) cudaStreamDestroy(b->st);
+        delete b;
+        return rc;
+    }
+    b->active.assign(count, 1);
+    b->built_version.assign(count, ~0u);
+    *out = b;
+    return 0;
+}
+
+int gpe_gb_batch_destroy(gpe_gb_batch* b) {
+    if (!b) return GPE_ERR_NO_ENGINE;
+    cudaStreamSynchronize(b->st);
+    gpe::batch_free_items(b);
+    for (auto* h : b->eng) gpe_gb_destroy(h);
+    cudaStreamDestroy(b->st);
+    delete b;
+    return gpe::cuda_rc(cudaGetLastError());
+}
+
+gpe_gb_engine* gpe_gb_batch_engine(gpe_gb_batch* b, int i) {
+    if (!b || i < 0 || i >= (int)b->eng.size()) return nullptr;
+    return b->eng[i];
+}
+
+int gpe_gb_batch_set_active(gpe_gb_batch* b, int i, int active) {
+    if (!b) return GPE_ERR_NO_ENGINE;
+    if (i < 0 || i >= (int)b->eng.size()) return GPE_ERR_ARGUMENT;
+    if ((b->active[i] != 0) != (active != 0)) b->dirty = true;
+    b->active[i] = active != 0;
+    return 0;
+}
+
+int gpe_gb_batch_evolve(gpe_gb_batch* b, int nt) {
+    if (!b) return GPE_ERR_NO_ENGINE;
+    return gpe::batch_evolve(b, nt);
+}
+
+int gpe_gb_batch_chemical_potentials(gpe_gb_batch* b, double* mu, double* dmu) {
+    if (!b || !mu || !dmu) return GPE_ERR_ARGUMENT;
+    const size_t n = b->eng.size();
+    std::vector<gpe::DynState> host(n);
+    for (size_t i = 0; i < n; i++)
+        GPE_CK(cudaMemcpyAsync(&host[i], b->eng[i]->e.dyn, sizeof(gpe::DynState), cudaMemcpyDeviceToHost, b->st));
+    GPE_CK(cudaStreamSynchronize(b->st));
+    for (size_t i = 0; i < n; i++) {
+        mu[i] = host[i].mu;
+        dmu[i] = host[i].dmu;
+    }
+    return 0;
+}
+
+long long gpe_gb_batch_kernel_launches(const gpe_gb_batch* b) { return b ? b->launches : -1; }
 
 const char* gpe_gb_error_string(int code) {
     switch (code) {

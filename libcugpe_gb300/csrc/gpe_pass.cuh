@@ -68,6 +68,7 @@ struct DynState {
     double s2;         // normalisation factor of psi2 inside an ITE step
     double norm;       // last sum of Gamma |psi|^2
     double mu;         // -0.5 log(norm / npart) / dt  (dev/gpe_engine.cu:1101)
+    double dmu;        // change of mu over the last step (ITE convergence test)
     double red[16];    // results of generic reductions
     unsigned int it;   // step counter since set_psi / set_time
     unsigned int ticket;
@@ -142,11 +143,11 @@ __device__ __forceinline__ void block_sum(double (&v)[NRED], double (*sred)[NRED
 // Last CTA of the grid: sums the per-CTA partials in index order with
 // Neumaier compensation and publishes the results.
 template <typename R, int NT>
-__device__ void finalize(const PassArgs<R>& a, double (*sred)[NRED]) {
+__device__ void finalize(const PassArgs<R>& a, double (*sred)[NRED], uint32_t nblk) {
     double s[NRED], c[NRED];
 #pragma unroll
     for (int r = 0; r < NRED; r++) { s[r] = 0.0; c[r] = 0.0; }
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += NT) {
+    for (int b = threadIdx.x; b < (int)nblk; b += NT) {
 #pragma unroll
         for (int r = 0; r < NRED; r++) {
             const double x = __ldcg(a.partials + (size_t)b * NRED + r);
@@ -165,7 +166,9 @@ __device__ void finalize(const PassArgs<R>& a, double (*sred)[NRED]) {
             if (a.flags & F_REDUCE) {
                 d->norm = s[0];
                 d->s_prev = sqrt(a.npart / s[0]);
-                d->mu = -.5 * log(s[0] / a.npart) / a.dt;
+                const double mu = -.5 * log(s[0] / a.npart) / a.dt;
+                d->dmu = mu - d->mu;
+                d->mu = mu;
             }
             d->it = d->it + 1;
         }
@@ -258,9 +261,10 @@ __host__ __device__ inline int op_class(int pre, int mid, int post, uint32_t fla
     return C_KIN;
 }
 
+// The pass over the pencils of one lattice, as CTA `blk` of `nblk` CTAs
+// working on it (a standalone launch, or one condensate of a batch).
 template <typename R, int N, int AX, int NT, int CLS>
-__global__ void __launch_bounds__(NT, PassGeom<R, N, AX, NT>::MINB)
-pass_kernel(const PassArgs<R> a) {
+__device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, uint32_t nblk) {
     using Geo = PassGeom<R, N, AX, NT>;
     constexpr int E = Geo::E, T = Geo::T, CW = Geo::CW, G = Geo::G, W = Geo::W, ROW = Geo::ROW;
     constexpr int SSTR = (AX == AX_Z) ? 1 : CW;
@@ -301,7 +305,7 @@ pass_kernel(const PassArgs<R> a) {
 
     // 32-bit point indices: the largest lattice (512^3) has 2^27 points.
     // CTAs past the last pencil (small lattices) compute on zeros and store nothing.
-    const uint32_t gp = blockIdx.x * (uint32_t)W + pl;  // pencil id
+    const uint32_t gp = blk * (uint32_t)W + pl;  // pencil id
     const bool valid = gp < a.npencils;
     const int ly = a.ly, lz = a.lz;
     uint32_t base, lstr;  // first point of the pencil, log2 of the point stride
@@ -553,18 +557,24 @@ pass_kernel(const PassArgs<R> a) {
             block_sum<NT>(acc, sred);
             if (tid == 0) {
 #pragma unroll
-                for (int r = 0; r < NRED; r++) a.partials[(size_t)blockIdx.x * NRED + r] = acc[r];
+                for (int r = 0; r < NRED; r++) a.partials[(size_t)blk * NRED + r] = acc[r];
                 __threadfence();
                 const unsigned prev = atomicAdd(&a.dyn->ticket, 1u);
-                last_cta = (prev == gridDim.x - 1);
+                last_cta = (prev == nblk - 1);
             }
             __syncthreads();
             if (last_cta) {
                 __threadfence();
-                finalize<R, NT>(a, sred);
+                finalize<R, NT>(a, sred, nblk);
             }
         }
     }
+}
+
+template <typename R, int N, int AX, int NT, int CLS>
+__global__ void __launch_bounds__(NT, PassGeom<R, N, AX, NT>::MINB)
+pass_kernel(const PassArgs<R> a) {
+    pass_body<R, N, AX, NT, CLS>(a, blockIdx.x, gridDim.x);
 }
 
 }  // namespace gpe

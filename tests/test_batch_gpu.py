@@ -1,0 +1,71 @@
+"""Batched solver: independent condensates of uneven lattice sizes stepped by
+one launch per fused pass.  Each condensate must evolve exactly as it does
+alone (same pass body, same CTA shape), with its own parameters, norm and mu."""
+import numpy as np
+import pytest
+
+import oracle
+import libcugpe_gb300 as g
+from libcugpe_gb300 import configs
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [(32, 32, 32), (64, 32, 32), (32, 64, 64), (64, 64, 64), (128, 32, 32)]
+
+
+def params_for(i):
+    rng = np.random.default_rng(100 + i)
+    w = 0.05 * rng.uniform(0.8, 1.25)
+    return [0.05, 0.05, w, rng.uniform(5.0, 20.0)]
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def test_batch_matches_single_engines_exactly(cuda_device, gpe_lib):
+    b = g.Batch(SHAPES, interactions=-1, alpha=0.0, beta=1.0, dt=0.05, npart=[1.0] * len(SHAPES))
+    singles, psis = [], []
+    for i, s in enumerate(SHAPES):
+        psi = configs.random_state(s, seed=30 + i)
+        psis.append(psi)
+        b.engines[i].set_user_params(params_for(i))
+        b.engines[i].set_psi(0.0, psi)
+        e = g.Engine(s, -1, 0.0, 1.0, 0.05, 1.0, precision=g.FP32)
+        e.set_user_params(params_for(i))
+        e.set_psi(0.0, psi)
+        singles.append(e)
+    b.evolve(37)
+    mu_b, dmu_b = b.chemical_potentials()
+    for i, e in enumerate(singles):
+        mu = e.evolve_qf(37)
+        assert np.array_equal(b.engines[i].get_psi()[1], e.get_psi()[1]), i
+        assert mu_b[i] == mu
+        assert b.engines[i].get_psi()[0] == pytest.approx(37 * 0.05)
+    assert b.kernel_launches() >= 37 * 6
+
+
+def test_batch_against_fp64_oracle_and_inactive(cuda_device, gpe_lib):
+    shapes = SHAPES[:3]
+    b = g.Batch(shapes, interactions=-1, alpha=0.0, beta=1.0, dt=0.05)
+    psis = []
+    for i, s in enumerate(shapes):
+        psis.append(configs.random_state(s, seed=40 + i))
+        b.engines[i].set_user_params(params_for(i))
+        b.engines[i].set_psi(0.0, psis[i])
+    b.set_active(1, False)
+    b.evolve(10)
+    assert np.array_equal(b.engines[1].get_psi()[1], psis[1].astype(np.complex64).astype(np.complex128))
+    for i in (0, 2):
+        o = oracle.Oracle(shapes[i], -1, 0.0, 1.0, 0.05, 1.0, threads=4)
+        o.set_user_params(params_for(i))
+        o.set_psi(0.0, psis[i])
+        o.evolve_qf(10)
+        assert rel(b.engines[i].get_psi()[1], o.get_psi()[1]) <= 2e-5 * 10
+
+
+def test_batch_rejects_unsupported(cuda_device, gpe_lib):
+    with pytest.raises(g.GPEError):
+        g.Batch([(16, 16, 16)], precision=g.FP32)
+    with pytest.raises(g.GPEError):
+        g.Batch([(32, 32, 32)], precision=g.FP64)
