@@ -151,6 +151,26 @@ int gpe_gb_batch_evolve(gpe_gb_batch* b, int nt);
 /* Per condensate: mu of the last step and its change over that step (ITE). */
 int gpe_gb_batch_chemical_potentials(gpe_gb_batch* b, double* mu, double* dmu);
 long long gpe_gb_batch_kernel_launches(const gpe_gb_batch* b);
+/* Optimal control (no reference counterpart): gradients of
+ *   L(c) = 1 - |<psi_target|psi(T)>|^2
+ * with respect to the controls c[s][k] of the time-sliced potential
+ *   Vext(x, step) = trap + sum_k c[s][k] basis_k(x),  s = min(step / steps_per_slice, nslices - 1),
+ * through the discrete real-time step of `engine` (FP64, real time, contact
+ * BEC, no friction), by a hand-written adjoint of the step with forward
+ * checkpoints every `checkpoint_every` steps (nsteps must be a multiple).
+ * basis: nbasis real fields (nbasis <= 32), lattice units; controls:
+ * nslices*nbasis, lattice units, row s = slice.  While the problem exists it
+ * owns the engine's time-sliced potential and uses the engine's psi as
+ * scratch. */
+typedef struct gpe_gb_control gpe_gb_control;
+int gpe_gb_control_create(gpe_gb_control** out, gpe_gb_engine* engine, int nbasis, const double* basis, int nslices,
+                          int steps_per_slice, int nsteps, int checkpoint_every, const double* psi_target);
+/* L(c) from psi0 (complex128 host array). */
+int gpe_gb_control_loss(gpe_gb_control* c, const double* controls, const double* psi0, double* loss);
+/* L(c) and dL/dc (nslices*nbasis doubles). */
+int gpe_gb_control_loss_grad(gpe_gb_control* c, const double* controls, const double* psi0, double* loss,
+                             double* grad);
+int gpe_gb_control_destroy(gpe_gb_control* c);
 /* Message for a return code. */
 const char* gpe_gb_error_string(int code);
 

@@ -45,7 +45,8 @@ C_ABI_SYMBOLS = [
     "gpe_gb_profile_passes", "gpe_gb_norm_noalloc", "gpe_gb_set_vortex", "gpe_gb_get_phase", "gpe_gb_set_phase",
     "gpe_gb_evolve_vortex", "gpe_gb_evolve_enforced_phase", "gpe_gb_batch_create", "gpe_gb_batch_destroy",
     "gpe_gb_batch_engine", "gpe_gb_batch_set_active", "gpe_gb_batch_evolve", "gpe_gb_batch_chemical_potentials",
-    "gpe_gb_batch_kernel_launches", "gpe_gb_chemical_potential",
+    "gpe_gb_batch_kernel_launches", "gpe_gb_chemical_potential", "gpe_gb_control_create", "gpe_gb_control_loss",
+    "gpe_gb_control_loss_grad", "gpe_gb_control_destroy",
 ]
 
 
@@ -105,6 +106,10 @@ def _lib():
             "gpe_gb_batch_chemical_potentials": (i, [vp, dp, dp]),
             "gpe_gb_batch_kernel_launches": (ctypes.c_longlong, [vp]),
             "gpe_gb_chemical_potential": (i, [vp, dp, dp]),
+            "gpe_gb_control_create": (i, [ctypes.POINTER(vp), vp, i, dp, i, i, i, i, dp]),
+            "gpe_gb_control_loss": (i, [vp, dp, dp, dp]),
+            "gpe_gb_control_loss_grad": (i, [vp, dp, dp, dp, dp]),
+            "gpe_gb_control_destroy": (i, [vp]),
             "gpe_gb_profile_passes": (i, [vp, i, ctypes.POINTER(ctypes.c_float), dp, ip, ip, i, ip]),
         }
         for name, (res, args) in sig.items():

@@ -732,6 +732,354 @@ static bool pow2_side(int v) { return v >= 8 && v <= 512 && (v & (v - 1)) == 0; 
 
 }  // namespace gpe
 
+
+namespace gpe {
+
+// ============================================================ adjoint
+// Gradients of L = 1 - |<psi_target|psi(T)>|^2 with respect to the controls of
+// a time-sliced potential Vext(x, t) = trap + sum_k c[s][k] G_k(x), s = the
+// time slice of step t, through the discrete real-time step (contact BEC, no
+// friction).  One step n (c3 = -i dt/2, K the unitary kinetic operator):
+//   V = Vext(n) + g|psi_n|^2, E = exp(c3 V), A = E psi_n, B = K A, P = E B,
+//   W = (V + Vext(n+1) + g|P|^2)/2, F = exp(c3 W), C = F psi_n, D = K C,
+//   psi_{n+1} = F D                         (dev/gpe_engine.cu:719-742, 770-797)
+// Cotangents z_bar = dL/dRe z + i dL/dIm z; for w = a z, z_bar = conj(a) w_bar;
+// for w = exp(c3 V) z with real V, V_bar += Re(c3 w conj(w_bar)); for rho = |z|^2,
+// z_bar += 2 rho_bar z; K^dagger is the kinetic pass with the conjugate table.
+// Forward states are kept at checkpoints every `ck` steps and each segment is
+// recomputed forward before its reverse sweep.
+
+struct Control {
+    Engine* e = nullptr;
+    int nbasis = 0, nslices = 0, sps = 1, ck = 100;
+    double* basis = nullptr;     // [nbasis][n]
+    double* controls = nullptr;  // [nslices][nbasis]
+    double* fields = nullptr;    // [nslices][n]
+    double2* target = nullptr;
+    double2* ckpt = nullptr;     // checkpoints
+    int nckpt = 0;
+    double2* seg = nullptr;      // [ck][n] states of the segment being reversed
+    double2* bar = nullptr;      // cotangent of psi
+    double2* bufA = nullptr;
+    double2* bufC = nullptr;
+    double* Vn = nullptr;
+    double* W = nullptr;
+    double* Wbar = nullptr;
+    double* Vbar = nullptr;
+    double2* ktc = nullptr;      // conjugate kinetic tables, nx + ny + nz
+    double* part = nullptr;      // [kCtlBlocks][nbasis]
+    double* grad = nullptr;      // [nslices][nbasis]
+    double2* ovl = nullptr;      // overlap partials [kCtlBlocks]
+};
+
+constexpr int kCtlBlocks = 512;
+constexpr int kCtlThreads = 256;
+constexpr int kCtlMaxBasis = 32;
+
+struct CtlArgs {
+    const double *vx, *vy, *vz, *fields;
+    int ly, lz, nslices, sps;
+    size_t n;
+    double c3y, g;
+};
+
+__device__ __forceinline__ int ctl_slice(const CtlArgs& a, unsigned it) {
+    int s = (int)(it / (unsigned)a.sps);
+    return s >= a.nslices ? a.nslices - 1 : s;
+}
+__device__ __forceinline__ double ctl_vext(const CtlArgs& a, size_t i, unsigned it) {
+    const int ix = (int)(i >> (a.ly + a.lz)), iy = (int)((i >> a.lz) & ((1u << a.ly) - 1)), iz = (int)(i & ((1u << a.lz) - 1));
+    return (a.vx[ix] + a.vy[iy]) + a.vz[iz] + a.fields[(size_t)ctl_slice(a, it) * a.n + i];
+}
+__device__ __forceinline__ double2 ctl_phase(double c3y, double V) {
+    double s, c;
+    sincos(c3y * V, &s, &c);
+    return make_double2(c, s);
+}
+// Re(c3 w conj(wb)) with c3 = i c3y
+__device__ __forceinline__ double ctl_vbar(double c3y, double2 w, double2 wb) {
+    return -c3y * (w.y * wb.x - w.x * wb.y);
+}
+
+__global__ void k_ctl_fields(const double* c, const double* basis, double* fields, int nslices, int nbasis, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        for (int s = 0; s < nslices; s++) {
+            double v = 0.0;
+            for (int k = 0; k < nbasis; k++) v += c[s * nbasis + k] * basis[(size_t)k * n + i];
+            fields[(size_t)s * n + i] = v;
+        }
+}
+
+// partial sums of conj(t) psi, then the last block publishes the overlap
+__global__ void k_ctl_overlap(const double2* t, const double2* p, size_t n, double2* part) {
+    __shared__ double sx[kCtlThreads], sy[kCtlThreads];
+    double ax = 0.0, ay = 0.0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double2 a = t[i], b = p[i];
+        ax += a.x * b.x + a.y * b.y;
+        ay += a.x * b.y - a.y * b.x;
+    }
+    sx[threadIdx.x] = ax;
+    sy[threadIdx.x] = ay;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) { sx[threadIdx.x] += sx[threadIdx.x + o]; sy[threadIdx.x] += sy[threadIdx.x + o]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = make_double2(sx[0], sy[0]);
+}
+
+__global__ void k_ctl_seed(const double2* t, double2* bar, size_t n, double2 o) {
+    // d(1 - |o|^2): bar = -2 o psi_target
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double2 a = t[i];
+        bar[i] = make_double2(-2.0 * (o.x * a.x - o.y * a.y), -2.0 * (o.x * a.y + o.y * a.x));
+    }
+}
+
+// V = Vext(n) + g|psi|^2 -> Vn ; A = exp(c3 V) psi -> bufA
+__global__ void k_ctl_fw1(CtlArgs a, unsigned it, const double2* psi, double* Vn, double2* A) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < a.n; i += (size_t)gridDim.x * blockDim.x) {
+        const double2 p = psi[i];
+        const double V = ctl_vext(a, i, it) + a.g * (p.x * p.x + p.y * p.y);
+        Vn[i] = V;
+        A[i] = cmul(p, ctl_phase(a.c3y, V));
+    }
+}
+
+// P = E B ; W = (V + Vext(n+1) + g|P|^2)/2 -> W ; C = exp(c3 W) psi -> bufC
+__global__ void k_ctl_fw2(CtlArgs a, unsigned it, const double2* psi, const double* Vn, const double2* B, double* W,
+                          double2* C) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < a.n; i += (size_t)gridDim.x * blockDim.x) {
+        const double V = Vn[i];
+        const double2 P = cmul(B[i], ctl_phase(a.c3y, V));
+        const double w = 0.5 * ((V + ctl_vext(a, i, it + 1)) + a.g * (P.x * P.x + P.y * P.y));
+        W[i] = w;
+        C[i] = cmul(psi[i], ctl_phase(a.c3y, w));
+    }
+}
+
+// psi_{n+1} = F D ; Wbar = Re(c3 psi_{n+1} conj(bar)) ; D_bar = conj(F) bar -> bufC
+__global__ void k_ctl_bw1(CtlArgs a, const double* W, double2* CD, const double2* bar, double* Wbar) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < a.n; i += (size_t)gridDim.x * blockDim.x) {
+        const double2 F = ctl_phase(a.c3y, W[i]);
+        const double2 nb = bar[i];
+        const double2 pn = cmul(F, CD[i]);
+        Wbar[i] = ctl_vbar(a.c3y, pn, nb);
+        CD[i] = cmulc(nb, F);
+    }
+}
+
+// with C_bar in bufC: bar = conj(F) C_bar ; W_bar += Re(c3 C conj(C_bar)) ;
+// V_bar = W_bar/2 ; Vext(n+1)_bar = W_bar/2 (projected) ; P = E B ;
+// P_bar = g W_bar P ; B_bar = conj(E) P_bar -> bufA ; V_bar += Re(c3 P conj(P_bar))
+__global__ void __launch_bounds__(kCtlThreads) k_ctl_bw2(CtlArgs a, const double2* psi, const double* Vn, const double* W,
+                                                        const double* Wbar, const double2* Cbar, double2* AB, double* Vbar,
+                                                        double2* bar, const double* basis, int nbasis, double* part) {
+    __shared__ double sp[kCtlMaxBasis][kCtlThreads / 32];
+    double acc[kCtlMaxBasis];
+    for (int k = 0; k < nbasis; k++) acc[k] = 0.0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < a.n; i += (size_t)gridDim.x * blockDim.x) {
+        const double2 F = ctl_phase(a.c3y, W[i]);
+        const double2 cb = Cbar[i];
+        const double2 C = cmul(F, psi[i]);
+        bar[i] = cmulc(cb, F);
+        const double wb = Wbar[i] + ctl_vbar(a.c3y, C, cb);
+        const double2 E = ctl_phase(a.c3y, Vn[i]);
+        const double2 P = cmul(AB[i], E);
+        const double2 Pb = make_double2(a.g * wb * P.x, a.g * wb * P.y);
+        AB[i] = cmulc(Pb, E);
+        Vbar[i] = 0.5 * wb + ctl_vbar(a.c3y, P, Pb);
+        for (int k = 0; k < nbasis; k++) acc[k] += basis[(size_t)k * a.n + i] * (0.5 * wb);
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int k = 0; k < nbasis; k++) {
+        double v = acc[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) sp[k][w] = v;
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < nbasis) {
+        double v = 0.0;
+        for (int j = 0; j < kCtlThreads / 32; j++) v += sp[threadIdx.x][j];
+        part[(size_t)blockIdx.x * nbasis + threadIdx.x] = v;
+    }
+}
+
+// with A_bar in bufA: bar += conj(E) A_bar ; V_bar += Re(c3 A conj(A_bar)) ;
+// Vext(n)_bar = V_bar (projected) ; bar += 2 g V_bar psi
+__global__ void __launch_bounds__(kCtlThreads) k_ctl_bw3(CtlArgs a, const double2* psi, const double* Vn,
+                                                        const double2* Abar, const double* Vbar, double2* bar,
+                                                        const double* basis, int nbasis, double* part) {
+    __shared__ double sp[kCtlMaxBasis][kCtlThreads / 32];
+    double acc[kCtlMaxBasis];
+    for (int k = 0; k < nbasis; k++) acc[k] = 0.0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < a.n; i += (size_t)gridDim.x * blockDim.x) {
+        const double2 E = ctl_phase(a.c3y, Vn[i]);
+        const double2 p = psi[i];
+        const double2 A = cmul(E, p);
+        const double2 ab = Abar[i];
+        const double vb = Vbar[i] + ctl_vbar(a.c3y, A, ab);
+        const double2 e = cmulc(ab, E);
+        double2 b = bar[i];
+        b.x += e.x + 2.0 * a.g * vb * p.x;
+        b.y += e.y + 2.0 * a.g * vb * p.y;
+        bar[i] = b;
+        for (int k = 0; k < nbasis; k++) acc[k] += basis[(size_t)k * a.n + i] * vb;
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int k = 0; k < nbasis; k++) {
+        double v = acc[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) sp[k][w] = v;
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < nbasis) {
+        double v = 0.0;
+        for (int j = 0; j < kCtlThreads / 32; j++) v += sp[threadIdx.x][j];
+        part[(size_t)blockIdx.x * nbasis + threadIdx.x] = v;
+    }
+}
+
+// grad[slice][k] += sum over blocks of part[b][k] (fixed order)
+__global__ void k_ctl_accumulate(const double* part, int nblocks, int nbasis, double* grad_row) {
+    const int k = threadIdx.x;
+    if (k >= nbasis) return;
+    double s = 0.0;
+    for (int b = 0; b < nblocks; b++) s += part[(size_t)b * nbasis + k];
+    grad_row[k] += s;
+}
+
+static CtlArgs ctl_args(const Control* c) {
+    const Engine* e = c->e;
+    CtlArgs a;
+    a.vx = (const double*)e->ax[0].vt;
+    a.vy = (const double*)e->ax[1].vt;
+    a.vz = (const double*)e->ax[2].vt;
+    a.fields = c->fields;
+    a.ly = e->l3[1];
+    a.lz = e->l3[2];
+    a.nslices = c->nslices;
+    a.sps = c->sps;
+    a.n = e->n;
+    double c3x, c3y;
+    step_coeff(e, &c3x, &c3y);
+    a.c3y = c3y;
+    a.g = 4 * M_PI * e->up[3];
+    return a;
+}
+
+// kinetic operator (conj = 0) or its adjoint (conj = 1) on buf, three axis passes
+static int ctl_kinetic(Control* c, double2* buf, int conj) {
+    Engine* e = c->e;
+    size_t off = 0;
+    for (int axis = 0; axis < 3; axis++) {
+        PassArgs<double> a = base_args<double>(e);
+        axis_args(e, a, axis);
+        if (conj) a.ktab = c->ktc + off;
+        a.ltab = (const double*)e->ax[axis].lqf;
+        a.in = buf;
+        a.out = buf;
+        a.pre = PRE_NONE; a.mid = MID_NONE; a.post = POST_NONE;
+        a.flags = F_KIN | F_STORE;
+        a.npencils = (uint32_t)pencils_of(e, axis);
+        e->launches++;
+        GPE_CK(launch_pass<double>(a, e->n3[axis], axis, pencils_of(e, axis), e->st));
+        off += (size_t)e->n3[axis];
+    }
+    return 0;
+}
+
+static int ctl_forward(Control* c, const double* controls_host, const double* psi0_host, double* loss, double2* o_out) {
+    Engine* e = c->e;
+    const size_t n = e->n;
+    GPE_CK(cudaMemcpyAsync(c->controls, controls_host, sizeof(double) * c->nslices * c->nbasis, cudaMemcpyHostToDevice, e->st));
+    k_ctl_fields<<<1024, 256, 0, e->st>>>(c->controls, c->basis, c->fields, c->nslices, c->nbasis, n);
+    GPE_CK(cudaGetLastError());
+    e->vextra = c->fields;
+    e->vslices = c->nslices;
+    e->vsteps = c->sps;
+    e->graph_dirty = true;
+    e->version++;
+    GPE_CK(cudaMemcpyAsync(e->psi, psi0_host, sizeof(double2) * n, cudaMemcpyHostToDevice, e->st));
+    e->t0 = 0.0;
+    e->it = 0;
+    GPE_RC(set_state(e, 0, 1.0));
+    const int nseg = c->nckpt - 1;
+    for (int j = 0; j < nseg; j++) {
+        GPE_CK(cudaMemcpyAsync(c->ckpt + (size_t)j * n, e->psi, sizeof(double2) * n, cudaMemcpyDeviceToDevice, e->st));
+        GPE_RC(evolve(e, c->ck, nullptr));
+    }
+    GPE_CK(cudaMemcpyAsync(c->ckpt + (size_t)nseg * n, e->psi, sizeof(double2) * n, cudaMemcpyDeviceToDevice, e->st));
+    k_ctl_overlap<<<kCtlBlocks, kCtlThreads, 0, e->st>>>(c->target, (const double2*)e->psi, n, c->ovl);
+    std::vector<double2> part(kCtlBlocks);
+    GPE_CK(cudaMemcpyAsync(part.data(), c->ovl, sizeof(double2) * kCtlBlocks, cudaMemcpyDeviceToHost, e->st));
+    GPE_CK(cudaStreamSynchronize(e->st));
+    double2 o = make_double2(0.0, 0.0);
+    for (int b = 0; b < kCtlBlocks; b++) { o.x += part[b].x; o.y += part[b].y; }
+    *loss = 1.0 - (o.x * o.x + o.y * o.y);
+    if (o_out) *o_out = o;
+    return 0;
+}
+
+static int ctl_backward(Control* c, double2 o, double* grad_host) {
+    Engine* e = c->e;
+    const size_t n = e->n;
+    const CtlArgs a = ctl_args(c);
+    const int nseg = c->nckpt - 1;
+    GPE_CK(cudaMemsetAsync(c->grad, 0, sizeof(double) * c->nslices * c->nbasis, e->st));
+    k_ctl_seed<<<1024, 256, 0, e->st>>>(c->target, c->bar, n, o);
+    for (int j = nseg - 1; j >= 0; j--) {
+        // recompute the segment's states forward from its checkpoint
+        GPE_CK(cudaMemcpyAsync(e->psi, c->ckpt + (size_t)j * n, sizeof(double2) * n, cudaMemcpyDeviceToDevice, e->st));
+        e->it = (unsigned)(j * c->ck);
+        GPE_RC(set_state(e, e->it, 1.0));
+        for (int i = 0; i < c->ck; i++) {
+            GPE_CK(cudaMemcpyAsync(c->seg + (size_t)i * n, e->psi, sizeof(double2) * n, cudaMemcpyDeviceToDevice, e->st));
+            GPE_RC(evolve(e, 1, nullptr));
+        }
+        for (int i = c->ck - 1; i >= 0; i--) {
+            const unsigned it = (unsigned)(j * c->ck + i);
+            const double2* psi = c->seg + (size_t)i * n;
+            k_ctl_fw1<<<1024, 256, 0, e->st>>>(a, it, psi, c->Vn, c->bufA);
+            GPE_RC(ctl_kinetic(c, c->bufA, 0));
+            k_ctl_fw2<<<1024, 256, 0, e->st>>>(a, it, psi, c->Vn, c->bufA, c->W, c->bufC);
+            GPE_RC(ctl_kinetic(c, c->bufC, 0));
+            k_ctl_bw1<<<1024, 256, 0, e->st>>>(a, c->W, c->bufC, c->bar, c->Wbar);
+            GPE_RC(ctl_kinetic(c, c->bufC, 1));
+            k_ctl_bw2<<<kCtlBlocks, kCtlThreads, 0, e->st>>>(a, psi, c->Vn, c->W, c->Wbar, c->bufC, c->bufA, c->Vbar,
+                                                          c->bar, c->basis, c->nbasis, c->part);
+            int s1 = (int)((it + 1) / (unsigned)c->sps);
+            if (s1 >= c->nslices) s1 = c->nslices - 1;
+            k_ctl_accumulate<<<1, kCtlMaxBasis, 0, e->st>>>(c->part, kCtlBlocks, c->nbasis, c->grad + (size_t)s1 * c->nbasis);
+            GPE_RC(ctl_kinetic(c, c->bufA, 1));
+            k_ctl_bw3<<<kCtlBlocks, kCtlThreads, 0, e->st>>>(a, psi, c->Vn, c->bufA, c->Vbar, c->bar, c->basis,
+                                                          c->nbasis, c->part);
+            int s0 = (int)(it / (unsigned)c->sps);
+            if (s0 >= c->nslices) s0 = c->nslices - 1;
+            k_ctl_accumulate<<<1, kCtlMaxBasis, 0, e->st>>>(c->part, kCtlBlocks, c->nbasis, c->grad + (size_t)s0 * c->nbasis);
+            e->launches += 8;
+            GPE_CK(cudaGetLastError());
+        }
+    }
+    GPE_CK(cudaMemcpyAsync(grad_host, c->grad, sizeof(double) * c->nslices * c->nbasis, cudaMemcpyDeviceToHost, e->st));
+    return cuda_rc(cudaStreamSynchronize(e->st));
+}
+
+static void ctl_release(Control* c) {
+    if (c->e && c->e->vextra == c->fields) {
+        c->e->vextra = nullptr;
+        c->e->vslices = 0;
+        c->e->graph_dirty = true;
+        c->e->version++;
+    }
+    cudaFree(c->basis); cudaFree(c->controls); cudaFree(c->fields); cudaFree(c->target); cudaFree(c->ckpt);
+    cudaFree(c->seg); cudaFree(c->bar); cudaFree(c->bufA); cudaFree(c->bufC); cudaFree(c->Vn); cudaFree(c->W);
+    cudaFree(c->Wbar); cudaFree(c->Vbar); cudaFree(c->ktc); cudaFree(c->part); cudaFree(c->grad); cudaFree(c->ovl);
+}
+
+}  // namespace gpe
+
 using gpe::Engine;
 
 // ===================================================================== C ABI
@@ -1304,6 +1652,98 @@ int gpe_gb_batch_chemical_potentials(gpe_gb_batch* b, double* mu, double* dmu) {
 }
 
 long long gpe_gb_batch_kernel_launches(const gpe_gb_batch* b) { return b ? b->launches : -1; }
+
+struct gpe_gb_control {
+    gpe::Control c;
+};
+
+int gpe_gb_control_create(gpe_gb_control** out, gpe_gb_engine* h, int nbasis, const double* basis, int nslices,
+                          int steps_per_slice, int nsteps, int checkpoint_every, const double* psi_target) {
+    if (!out || !h || !basis || !psi_target) return GPE_ERR_ARGUMENT;
+    *out = nullptr;
+    Engine* e = &h->e;
+    if (e->prec != GPE_PRECISION_FP64 || e->beta != 0.0 || e->alpha == 0.0 || e->inter != gpe::INTER_BEC ||
+        e->qf_raw != 0.0)
+        return GPE_ERR_ARGUMENT;
+    if (nbasis <= 0 || nbasis > gpe::kCtlMaxBasis || nslices <= 0 || steps_per_slice <= 0 || checkpoint_every <= 0 ||
+        nsteps <= 0 || nsteps % checkpoint_every != 0)
+        return GPE_ERR_ARGUMENT;
+    gpe_gb_control* hc = new (std::nothrow) gpe_gb_control();
+    if (!hc) return GPE_ERR_ARGUMENT;
+    gpe::Control* c = &hc->c;
+    c->e = e;
+    c->nbasis = nbasis;
+    c->nslices = nslices;
+    c->sps = steps_per_slice;
+    c->ck = checkpoint_every;
+    c->nckpt = nsteps / checkpoint_every + 1;
+    const size_t n = e->n;
+    int rc = 0;
+    auto alloc = [&](void** p, size_t bytes) {
+        if (!rc) { cudaError_t ce = cudaMalloc(p, bytes); if (ce != cudaSuccess) rc = (int)ce; }
+    };
+    alloc((void**)&c->basis, sizeof(double) * nbasis * n);
+    alloc((void**)&c->controls, sizeof(double) * nslices * nbasis);
+    alloc((void**)&c->fields, sizeof(double) * nslices * n);
+    alloc((void**)&c->target, sizeof(double2) * n);
+    alloc((void**)&c->ckpt, sizeof(double2) * n * c->nckpt);
+    alloc((void**)&c->seg, sizeof(double2) * n * c->ck);
+    alloc((void**)&c->bar, sizeof(double2) * n);
+    alloc((void**)&c->bufA, sizeof(double2) * n);
+    alloc((void**)&c->bufC, sizeof(double2) * n);
+    alloc((void**)&c->Vn, sizeof(double) * n);
+    alloc((void**)&c->W, sizeof(double) * n);
+    alloc((void**)&c->Wbar, sizeof(double) * n);
+    alloc((void**)&c->Vbar, sizeof(double) * n);
+    alloc((void**)&c->ktc, sizeof(double2) * (e->n3[0] + e->n3[1] + e->n3[2]));
+    alloc((void**)&c->part, sizeof(double) * gpe::kCtlBlocks * nbasis);
+    alloc((void**)&c->grad, sizeof(double) * nslices * nbasis);
+    alloc((void**)&c->ovl, sizeof(double2) * gpe::kCtlBlocks);
+    if (!rc) {
+        cudaError_t ce = cudaMemcpy(c->basis, basis, sizeof(double) * nbasis * n, cudaMemcpyHostToDevice);
+        if (ce == cudaSuccess) ce = cudaMemcpy(c->target, psi_target, sizeof(double2) * n, cudaMemcpyHostToDevice);
+        if (ce != cudaSuccess) rc = (int)ce;
+    }
+    if (!rc) {  // conjugate kinetic tables
+        std::vector<double2> t;
+        for (int a = 0; a < 3; a++) {
+            std::vector<double2> row(e->n3[a]);
+            cudaMemcpy(row.data(), e->ax[a].ktab, sizeof(double2) * e->n3[a], cudaMemcpyDeviceToHost);
+            for (auto& v : row) v.y = -v.y;
+            t.insert(t.end(), row.begin(), row.end());
+        }
+        cudaError_t ce = cudaMemcpy(c->ktc, t.data(), sizeof(double2) * t.size(), cudaMemcpyHostToDevice);
+        if (ce != cudaSuccess) rc = (int)ce;
+    }
+    if (rc) {
+        gpe::ctl_release(c);
+        delete hc;
+        return rc;
+    }
+    *out = hc;
+    return 0;
+}
+
+int gpe_gb_control_loss(gpe_gb_control* hc, const double* controls, const double* psi0, double* loss) {
+    if (!hc || !controls || !psi0 || !loss) return GPE_ERR_ARGUMENT;
+    return gpe::ctl_forward(&hc->c, controls, psi0, loss, nullptr);
+}
+
+int gpe_gb_control_loss_grad(gpe_gb_control* hc, const double* controls, const double* psi0, double* loss,
+                             double* grad) {
+    if (!hc || !controls || !psi0 || !loss || !grad) return GPE_ERR_ARGUMENT;
+    double2 o;
+    GPE_RC(gpe::ctl_forward(&hc->c, controls, psi0, loss, &o));
+    return gpe::ctl_backward(&hc->c, o, grad);
+}
+
+int gpe_gb_control_destroy(gpe_gb_control* hc) {
+    if (!hc) return GPE_ERR_NO_ENGINE;
+    cudaStreamSynchronize(hc->c.e->st);
+    gpe::ctl_release(&hc->c);
+    delete hc;
+    return gpe::cuda_rc(cudaGetLastError());
+}
 
 const char* gpe_gb_error_string(int code) {
     switch (code) {

@@ -32,6 +32,10 @@ template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
     C c; c.x = a.x * b.x - a.y * b.y; c.y = a.x * b.y + a.y * b.x; return c;
 }
 template <typename C, typename S> __device__ __forceinline__ C cscale(C a, S s) { a.x = s * a.x; a.y = s * a.y; return a; }
+// a * conj(b)
+template <typename C> __device__ __forceinline__ C cmulc(C a, C b) {
+    C c; c.x = a.x * b.x + a.y * b.y; c.y = a.y * b.x - a.x * b.y; return c;
+}
 
 // cos and sin of 2 pi m / 16
 __host__ __device__ __forceinline__ constexpr double cos16(int m) {
