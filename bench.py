@@ -396,6 +396,69 @@ def run_batch_workload(args):
     print(json.dumps(line), flush=True)
 
 
+def run_control_workload(args):
+    """Optimal control, 64^3 real-time BEC (gN=200, dt=1e-3, 2000 steps, 16 Gaussians x 100 slices):
+    adjoint gradient timing and its check against central differences at 20 seeded controls."""
+    import libcugpe_gb300 as g
+    from libcugpe_gb300 import configs
+    from libcugpe_gb300.control import ControlProblem
+    n, dx, gN, dt_phys, nsteps, nsl, nb, sigma = 64, 0.25, 200.0, 1e-3, args.control_steps, 100, 16, 0.8
+    rng = np.random.default_rng(0)
+    shape = (n, n, n)
+    w = dx * dx
+    params = [w, w, w, gN / dx / (4 * np.pi)]
+    dt = dt_phys / (dx * dx)
+    X, Y, Z = configs.grid(shape, dx)
+    centres = rng.uniform(-3, 3, (nb, 3))
+    basis = np.stack([np.exp(-((X - c[0]) ** 2 + (Y - c[1]) ** 2 + (Z - c[2]) ** 2) / (2 * sigma * sigma))
+                      for c in centres]) * (dx * dx)  # lattice energy units per unit physical control
+    c_phys = 0.05 * rng.standard_normal((nsl, nb))
+
+    def ground_state(shift):
+        e = g.Engine(shape, -1, 0.0, 1.0, dt * 20, 1.0, precision=g.FP64)
+        e.set_user_params(params)
+        if shift:  # trap centred at x = shift: 0.5 (x - s)^2 - 0.5 x^2 = -s x + s^2/2
+            e.set_potential_slices(((-shift * X + 0.5 * shift * shift) * dx * dx)[None], 1)
+        e.set_psi(0.0, configs.normalise(np.exp(-((X - shift) ** 2 + Y * Y + Z * Z) / 2).astype(np.complex128), 1, 1))
+        for _ in range(40):
+            e.evolve_qf(100)
+        psi = e.get_psi()[1]
+        e.close()
+        return psi
+
+    psi0, target = ground_state(0.0), ground_state(0.5)
+    e = g.Engine(shape, -1, 1.0, 0.0, dt, 1.0, precision=g.FP64)
+    e.set_user_params(params)
+    cp = ControlProblem(e, basis, nsl, nsteps // nsl, nsteps, target, checkpoint_every=args.control_ckpt)
+    t0 = time.perf_counter()
+    loss = cp.loss(c_phys, psi0)
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    loss2, grad = cp.loss_and_grad(c_phys, psi0)
+    t_grad = time.perf_counter() - t0
+    h = 1e-4
+    errs = []
+    picks = [(int(rng.integers(nsl)), int(rng.integers(nb))) for _ in range(args.control_fd)]
+    for s_, k_ in picks:
+        cpl, cmi = c_phys.copy(), c_phys.copy()
+        cpl[s_, k_] += h
+        cmi[s_, k_] -= h
+        fd = (cp.loss(cpl, psi0) - cp.loss(cmi, psi0)) / (2 * h)
+        errs.append({"slice": s_, "basis": k_, "adjoint": float(grad[s_, k_]), "fd": float(fd),
+                     "rel_err": float(abs(fd - grad[s_, k_]) / max(abs(grad[s_, k_]), 1e-30))})
+    line = {"metric": "optimal-control loss+gradient (64^3 RTE BEC, 2000 steps, 1600 controls) per second",
+            "value": 1.0 / t_grad, "unit": "gradients/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f64",
+            "data": "synthetic (seeded)", "loss": loss2, "loss_forward_only": loss, "forward_seconds": t_fwd,
+            "forward_plus_adjoint_seconds": t_grad, "grad_norm": float(np.linalg.norm(grad)),
+            "fd_check": {"h": h, "controls": len(errs), "max_rel_err": max(e_["rel_err"] for e_ in errs),
+                         "median_rel_err": float(np.median([e_["rel_err"] for e_ in errs])), "points": errs},
+            "config": {"workload": "config 4: 64^3, dx=0.25, gN=200, omega=1, dt=1e-3, 2000 steps, 16 Gaussians "
+                                   "sigma=0.8 centres U[-3,3]^3, 100 slices, controls N(0,0.05), target = ground state "
+                                   "of the trap shifted by (0.5,0,0), checkpoints every 100 steps"}}
+    print(json.dumps(line), flush=True)
+    cp.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -408,12 +471,18 @@ def main():
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--ite-steps", type=int, default=200)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--workload", default="ufg_qf", choices=["ufg_qf", "batch"])
+    ap.add_argument("--workload", default="ufg_qf", choices=["ufg_qf", "batch", "control"])
+    ap.add_argument("--control-steps", type=int, default=2000)
+    ap.add_argument("--control-ckpt", type=int, default=100)
+    ap.add_argument("--control-fd", type=int, default=20)
     ap.add_argument("--batch-max-steps", type=int, default=20000)
     ap.add_argument("--batch-serial-subset", type=int, default=2)
     args = ap.parse_args()
     if args.workload == "batch":
         run_batch_workload(args)
+        return
+    if args.workload == "control":
+        run_control_workload(args)
         return
     ws, rank, local = dist_setup()
     if args.impl == "reference":
