@@ -313,16 +313,19 @@ def batch_ensemble(seed=0, counts=((32, 32), (64, 48), (128, 16)), box=16.0, dt=
 
 
 def solve_until(evolve, chem, dx2, tol, check, max_steps):
-    """Steps in chunks of `check` until the mean per-step change of mu over the
-    chunk is below tol (physical units), or max_steps."""
-    steps, prev = 0, None
+    """Steps in chunks of `check` until the interval-mean mu changes by less than
+    tol per step (physical units) between consecutive chunks, or max_steps."""
+    steps, prev_sum, prev_mean = 0, None, None
     while steps < max_steps:
         evolve(check)
         steps += check
-        mu, _ = chem()
-        if prev is not None and abs(mu - prev) / check / dx2 < tol:
-            return steps, mu / dx2
-        prev = mu
+        mu, mu_sum = chem()
+        if prev_sum is not None:
+            mean = (mu_sum - prev_sum) / check
+            if prev_mean is not None and abs(mean - prev_mean) / check / dx2 < tol:
+                return steps, mean / dx2
+            prev_mean = mean
+        prev_sum = mu_sum
     return steps, None
 
 
@@ -341,7 +344,9 @@ def run_batch_workload(args):
     done = np.zeros(len(ens), dtype=bool)
     steps = np.zeros(len(ens), dtype=int)
     mu_final = np.full(len(ens), np.nan)
-    mu_prev = np.full(len(ens), np.nan)
+    sum_prev = np.full(len(ens), np.nan)
+    mean_prev = np.full(len(ens), np.nan)
+    last_change = np.full(len(ens), np.nan)
     torch.cuda.synchronize()
     l0 = b.kernel_launches()
     t0 = time.perf_counter()
@@ -349,18 +354,37 @@ def run_batch_workload(args):
     while not done.all() and total < max_steps:
         b.evolve(check)
         total += check
-        mu, _ = b.chemical_potentials()
+        _, msum = b.chemical_potentials()
         for i in np.nonzero(~done)[0]:
             steps[i] += check
-            # mean per-step change over the check interval: the FP32 field makes the
-            # single-step change jitter at ~1e-7, the mean over the interval does not
-            if np.isfinite(mu_prev[i]) and abs(mu[i] - mu_prev[i]) / check / dx2[i] < tol:
-                done[i] = True
-                mu_final[i] = mu[i] / dx2[i]
-                b.set_active(int(i), False)
-            mu_prev[i] = mu[i]
+            # the mu of one step from an FP32 field jitters at ~1e-7; the change of the
+            # interval mean (mean of `check` steps) between intervals does not
+            if np.isfinite(sum_prev[i]):
+                mean = (msum[i] - sum_prev[i]) / check
+                if np.isfinite(mean_prev[i]):
+                    last_change[i] = abs(mean - mean_prev[i]) / check / dx2[i]
+                    if last_change[i] < tol:
+                        done[i] = True
+                        mu_final[i] = mean / dx2[i]
+                        b.set_active(int(i), False)
+                mean_prev[i] = mean
+            sum_prev[i] = msum[i]
     t_batch = time.perf_counter() - t0
     launches = b.kernel_launches() - l0
+    # the unconverged: their last interval change, and what FP64 needs on the same problem
+    stragglers = []
+    for i in np.nonzero(~done)[0][: args.batch_diag]:
+        c = ens[i]
+        e = g.Engine(c["shape"], -1, 0.0, 1.0, c["dt"], 1.0, precision=g.FP64)
+        e.set_user_params(c["params"])
+        e.set_psi(0.0, c["psi"])
+        st64, mu64 = solve_until(e.evolve_qf, e.chemical_potential, c["dx"] ** 2, tol, check, max_steps)
+        e.close()
+        stragglers.append({"n": c["shape"][0], "gN": c["params"][3] * c["dx"] * 4 * np.pi,
+                           "omega_ratio": c["params"][2] / c["params"][0], "fp32_steps": int(steps[i]),
+                           "fp32_last_change_per_step": float(last_change[i]),
+                           "fp64_steps_to_converge": int(st64),
+                           "fp32_vs_fp64_mu": float(abs(mean_prev[i] / dx2[i] - mu64) / abs(mu64)) if mu64 else None})
     # serial FP64 loop: one condensate at a time, same criterion; a stated subset per size
     per_size = {}
     subset = args.batch_serial_subset
@@ -390,9 +414,50 @@ def run_batch_workload(args):
                             "how": f"FP64 engine, one condensate at a time, first {subset} of each size timed; "
                                    "the others take the mean of their size"},
             "speedup_vs_serial_fp64": t_serial / t_batch,
+            "fp32_steps_to_converge": {str(n): [int(x) for x in np.percentile(steps[[j for j, c in enumerate(ens)
+                                                  if c["shape"][0] == n and done[j]]], [50, 90, 100])]
+                                       if any(done[j] for j, c in enumerate(ens) if c["shape"][0] == n) else None
+                                       for n in sorted({c["shape"][0] for c in ens})},
+            "unconverged": stragglers,
             "config": {"workload": "config 3: BEC ITE, gN~U[50,500], omega_z/omega_perp~U[0.8,1.25], "
-                                   "width~U[0.8,1.2], box 16 (dx=16/n), dt=5e-3; converged when the mean per-step "
-                                   "change of mu over a 25-step interval is < 1e-8"}}
+                                   "width~U[0.8,1.2], box 16 (dx=16/n), dt=5e-3; converged when the mean of mu over a "
+                                   "25-step interval changes by < 1e-8 per step between intervals"}}
+    print(json.dumps(line), flush=True)
+
+
+def run_bec64_workload(args):
+    """64^3 BEC imaginary-time ground state (FP64, 2000 steps, mu every step), against the
+    reference engine on the same GPU and the CPU oracle."""
+    import libcugpe_gb300 as g
+    from libcugpe_gb300 import configs
+    w = configs.bec_ground_state_ite(n=64, steps=2000)
+    e = g.Engine(w.shape, -1, 0.0, 1.0, w.dt, w.npart, precision=g.FP64)
+    e.set_user_params(w.params)
+    e.set_psi(0.0, w.psi0)
+    e.normalize_psi()
+    e.evolve_qf(20)
+    e.set_psi(0.0, w.psi0)
+    e.normalize_psi()
+    t0 = time.perf_counter()
+    mu = e.evolve_qf(w.steps)
+    t_ours = time.perf_counter() - t0
+    en = e.energy()
+    line = {"metric": "64^3 BEC ITE steps/s (FP64 drop-in)", "value": w.steps / t_ours, "unit": "steps/s",
+            "n_gpus": 1, "higher_is_better": True, "dtype": "f64", "data": "synthetic (seeded)",
+            "mu": mu, "energy_per_particle": sum(en[1:]),
+            "config": {"workload": "config 1: 64^3, dx=0.25, omega=1, gN=100, ITE dt=1e-3, 2000 steps, "
+                                   "Gaussian width 1 x (1+0.01u)"}}
+    try:
+        from oracle import build_ref, ref_run
+        if ref_run.available():
+            build_ref.build_one(64, 64, 64, -1)
+            out = ref_run.run(w.shape, -1, 0.0, 1.0, w.dt, w.npart, w.params, w.psi0,
+                              ["N", "S20", "N", f"B{w.steps}", "E"])
+            line["reference_gpu"] = {"value": w.steps / (out["time_ms"][0] / 1e3), "unit": "steps/s",
+                                     "what": "reference libcugpe (cuFFT Z2Z) for sm_103a, mu requested every step "
+                                             "(its synchronous D2H per step)"}
+    except Exception as ex:
+        line["reference_gpu"] = {"unavailable": str(ex)[:200]}
     print(json.dumps(line), flush=True)
 
 
@@ -471,18 +536,22 @@ def main():
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--ite-steps", type=int, default=200)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--workload", default="ufg_qf", choices=["ufg_qf", "batch", "control"])
+    ap.add_argument("--workload", default="ufg_qf", choices=["ufg_qf", "batch", "control", "bec64"])
     ap.add_argument("--control-steps", type=int, default=2000)
     ap.add_argument("--control-ckpt", type=int, default=100)
     ap.add_argument("--control-fd", type=int, default=20)
     ap.add_argument("--batch-max-steps", type=int, default=20000)
     ap.add_argument("--batch-serial-subset", type=int, default=2)
+    ap.add_argument("--batch-diag", type=int, default=4)
     args = ap.parse_args()
     if args.workload == "batch":
         run_batch_workload(args)
         return
     if args.workload == "control":
         run_control_workload(args)
+        return
+    if args.workload == "bec64":
+        run_bec64_workload(args)
         return
     ws, rank, local = dist_setup()
     if args.impl == "reference":

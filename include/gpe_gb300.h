@@ -93,9 +93,10 @@ int gpe_gb_get_psi_device(gpe_gb_engine* e, double* t, void* psi);
 /* The CUDA stream (cudaStream_t) this engine launches on, for callers that
  * order their own work or events against it. */
 void* gpe_gb_get_stream(const gpe_gb_engine* e);
-/* mu of the last ITE step and its change over that step (the reference
- * returns mu through gpe_evolve_qf only; this also serves convergence tests). */
-int gpe_gb_chemical_potential(gpe_gb_engine* e, double* mu, double* dmu);
+/* mu of the last ITE step and the running sum of mu over all ITE steps of
+ * this engine (differences of the sum give interval means; the reference
+ * returns mu through gpe_evolve_qf only). */
+int gpe_gb_chemical_potential(gpe_gb_engine* e, double* mu, double* mu_sum);
 /* Runs all queued work to completion. */
 int gpe_gb_synchronize(gpe_gb_engine* e);
 /* Number of kernels this engine has launched so far. */
@@ -148,8 +149,8 @@ gpe_gb_engine* gpe_gb_batch_engine(gpe_gb_batch* b, int i);
 int gpe_gb_batch_set_active(gpe_gb_batch* b, int i, int active);
 /* nt steps of every active condensate (gpe_evolve_qf semantics per condensate). */
 int gpe_gb_batch_evolve(gpe_gb_batch* b, int nt);
-/* Per condensate: mu of the last step and its change over that step (ITE). */
-int gpe_gb_batch_chemical_potentials(gpe_gb_batch* b, double* mu, double* dmu);
+/* Per condensate: mu of the last ITE step and the running sum of mu. */
+int gpe_gb_batch_chemical_potentials(gpe_gb_batch* b, double* mu, double* mu_sum);
 long long gpe_gb_batch_kernel_launches(const gpe_gb_batch* b);
 /* Optimal control (no reference counterpart): gradients of
  *   L(c) = 1 - |<psi_target|psi(T)>|^2

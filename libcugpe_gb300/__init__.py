@@ -246,10 +246,10 @@ class Engine:
         return mu.value
 
     def chemical_potential(self):
-        """(mu, change of mu) of the last ITE step."""
-        mu, dmu = ctypes.c_double(), ctypes.c_double()
-        _check(_lib().gpe_gb_chemical_potential(self._h, ctypes.byref(mu), ctypes.byref(dmu)), "chemical_potential")
-        return mu.value, dmu.value
+        """(mu of the last ITE step, running sum of mu over all ITE steps)."""
+        mu, ms = ctypes.c_double(), ctypes.c_double()
+        _check(_lib().gpe_gb_chemical_potential(self._h, ctypes.byref(mu), ctypes.byref(ms)), "chemical_potential")
+        return mu.value, ms.value
 
     def energy(self):
         t, a, b, c = (ctypes.c_double() for _ in range(4))
@@ -322,11 +322,12 @@ class Batch:
         _check(_lib().gpe_gb_batch_set_active(self._h, int(i), 1 if active else 0), "batch_set_active")
 
     def chemical_potentials(self):
+        """Per condensate: (mu of the last ITE step, running sum of mu)."""
         n = len(self.engines)
         mu = np.zeros(n)
-        dmu = np.zeros(n)
-        _check(_lib().gpe_gb_batch_chemical_potentials(self._h, _dp(mu), _dp(dmu)), "batch_chemical_potentials")
-        return mu, dmu
+        ms = np.zeros(n)
+        _check(_lib().gpe_gb_batch_chemical_potentials(self._h, _dp(mu), _dp(ms)), "batch_chemical_potentials")
+        return mu, ms
 
     def kernel_launches(self) -> int:
         return int(_lib().gpe_gb_batch_kernel_launches(self._h))

@@ -1445,14 +1445,14 @@ int gpe_gb_energy(gpe_gb_engine* h, double* t, double* ekin, double* eint, doubl
                                          : gpe::energy<double>(e, ekin, eint, eext);
 }
 
-int gpe_gb_chemical_potential(gpe_gb_engine* h, double* mu, double* dmu) {
+int gpe_gb_chemical_potential(gpe_gb_engine* h, double* mu, double* mu_sum) {
     if (!h) return GPE_ERR_NO_ENGINE;
-    if (!mu || !dmu) return GPE_ERR_ARGUMENT;
+    if (!mu || !mu_sum) return GPE_ERR_ARGUMENT;
     gpe::DynState d;
     GPE_CK(cudaMemcpyAsync(&d, h->e.dyn, sizeof d, cudaMemcpyDeviceToHost, h->e.st));
     GPE_CK(cudaStreamSynchronize(h->e.st));
     *mu = d.mu;
-    *dmu = d.dmu;
+    *mu_sum = d.mu_sum;
     return 0;
 }
 
@@ -1637,8 +1637,8 @@ int gpe_gb_batch_evolve(gpe_gb_batch* b, int nt) {
     return gpe::batch_evolve(b, nt);
 }
 
-int gpe_gb_batch_chemical_potentials(gpe_gb_batch* b, double* mu, double* dmu) {
-    if (!b || !mu || !dmu) return GPE_ERR_ARGUMENT;
+int gpe_gb_batch_chemical_potentials(gpe_gb_batch* b, double* mu, double* mu_sum) {
+    if (!b || !mu || !mu_sum) return GPE_ERR_ARGUMENT;
     const size_t n = b->eng.size();
     std::vector<gpe::DynState> host(n);
     for (size_t i = 0; i < n; i++)
@@ -1646,7 +1646,7 @@ int gpe_gb_batch_chemical_potentials(gpe_gb_batch* b, double* mu, double* dmu) {
     GPE_CK(cudaStreamSynchronize(b->st));
     for (size_t i = 0; i < n; i++) {
         mu[i] = host[i].mu;
-        dmu[i] = host[i].dmu;
+        mu_sum[i] = host[i].mu_sum;
     }
     return 0;
 }

@@ -68,7 +68,8 @@ struct DynState {
     double s2;         // normalisation factor of psi2 inside an ITE step
     double norm;       // last sum of Gamma |psi|^2
     double mu;         // -0.5 log(norm / npart) / dt  (dev/gpe_engine.cu:1101)
-    double dmu;        // change of mu over the last step (ITE convergence test)
+    double dmu;        // change of mu over the last step
+    double mu_sum;     // running sum of mu over ITE steps (interval means for convergence tests)
     double red[16];    // results of generic reductions
     unsigned int it;   // step counter since set_psi / set_time
     unsigned int ticket;
@@ -169,6 +170,7 @@ __device__ void finalize(const PassArgs<R>& a, double (*sred)[NRED], uint32_t nb
                 const double mu = -.5 * log(s[0] / a.npart) / a.dt;
                 d->dmu = mu - d->mu;
                 d->mu = mu;
+                d->mu_sum += mu;
             }
             d->it = d->it + 1;
         }

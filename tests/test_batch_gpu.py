@@ -36,7 +36,7 @@ def test_batch_matches_single_engines_exactly(cuda_device, gpe_lib):
         e.set_psi(0.0, psi)
         singles.append(e)
     b.evolve(37)
-    mu_b, dmu_b = b.chemical_potentials()
+    mu_b, _ = b.chemical_potentials()
     for i, e in enumerate(singles):
         mu = e.evolve_qf(37)
         assert np.array_equal(b.engines[i].get_psi()[1], e.get_psi()[1]), i
