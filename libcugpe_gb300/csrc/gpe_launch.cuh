@@ -8,11 +8,17 @@
 
 namespace gpe {
 
-// Threads per CTA: 128, or one pencil group when a group is larger.  A
-// lattice with fewer pencils than a CTA holds runs a partial last CTA.
+// Threads per CTA: 128, or one pencil group of the wanted column width when
+// a group is larger (x and y pencils of 256 and 512 points in the FP32 form).
+// A lattice with fewer pencils than a CTA holds runs a partial last CTA.
 template <typename R, int N, int AX> constexpr int pass_nt() {
-    constexpr int g = PassGeom<R, N, AX, 128>::G;
-    return g > 128 ? g : 128;
+    if constexpr (AX == AX_Z) {
+        return 128;
+    } else {
+        constexpr int T = N / Plan<N>::E;
+        constexpr int want = ((32 / T) > cw_target<R, N, AX>()) ? (32 / T) : cw_target<R, N, AX>();
+        return (T * want > 128) ? T * want : 128;
+    }
 }
 
 template <typename R, int N, int AX, int NT, int CLS>

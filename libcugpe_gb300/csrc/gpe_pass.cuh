@@ -119,21 +119,21 @@ template <typename R> __device__ __forceinline__ R vext_at(const PassArgs<R>& a,
 
 template <typename C> __device__ __forceinline__ C ldc(const C* p) { return *p; }
 
-// Deterministic block sum of NRED doubles; result valid in thread 0.
-template <int NT>
+// Deterministic block sum of the first NR of NRED doubles; result valid in thread 0.
+template <int NT, int NR>
 __device__ __forceinline__ void block_sum(double (&v)[NRED], double (*sred)[NRED]) {
 #pragma unroll
-    for (int r = 0; r < NRED; r++)
+    for (int r = 0; r < NR; r++)
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v[r] += __shfl_down_sync(0xffffffffu, v[r], o);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (lane == 0)
 #pragma unroll
-        for (int r = 0; r < NRED; r++) sred[w][r] = v[r];
+        for (int r = 0; r < NR; r++) sred[w][r] = v[r];
     __syncthreads();
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int r = 0; r < NRED; r++) {
+        for (int r = 0; r < NR; r++) {
             double s = 0.0;
             for (int i = 0; i < (NT + 31) / 32; i++) s += sred[i][r];
             v[r] = s;
@@ -141,25 +141,62 @@ __device__ __forceinline__ void block_sum(double (&v)[NRED], double (*sred)[NRED
     }
 }
 
-// Last CTA of the grid: sums the per-CTA partials in index order with
-// Neumaier compensation and publishes the results.
-template <typename R, int NT>
-__device__ void finalize(const PassArgs<R>& a, double (*sred)[NRED], uint32_t nblk) {
-    double s[NRED], c[NRED];
+// Float-float (unevaluated hi + lo) sums for the FP32 form's norm partials.
+// FP64 arithmetic runs at a small fraction of the FP32 rate on this part, so
+// per-point FP64 accumulation would cost more than the transforms; a
+// float-float sum (Knuth's two-sum, Dekker's renormalisation) keeps ~44 bits
+// on the FP32 pipes.  Result as a double in thread 0.
+struct FF { float h, l; };
+__device__ __forceinline__ FF ff_add(FF a, float b) {
+    const float s = a.h + b, bb = s - a.h;
+    const float e = (a.h - (s - bb)) + (b - bb) + a.l;
+    FF r; r.h = s + e; r.l = e - (r.h - s); return r;
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+    const float s = a.h + b.h, bb = s - a.h;
+    const float e = (a.h - (s - bb)) + (b.h - bb) + (a.l + b.l);
+    FF r; r.h = s + e; r.l = e - (r.h - s); return r;
+}
+template <int NT>
+__device__ __forceinline__ double block_sum_ff(FF v, double (*sred)[NRED]) {
 #pragma unroll
-    for (int r = 0; r < NRED; r++) { s[r] = 0.0; c[r] = 0.0; }
-    for (int b = threadIdx.x; b < (int)nblk; b += NT) {
-#pragma unroll
-        for (int r = 0; r < NRED; r++) {
-            const double x = __ldcg(a.partials + (size_t)b * NRED + r);
-            const double t = s[r] + x;
-            c[r] += (fabs(s[r]) >= fabs(x)) ? (s[r] - t) + x : (x - t) + s[r];
-            s[r] = t;
-        }
+    for (int o = 16; o > 0; o >>= 1) {
+        FF u;
+        u.h = __shfl_down_sync(0xffffffffu, v.h, o);
+        u.l = __shfl_down_sync(0xffffffffu, v.l, o);
+        v = ff_add(v, u);
     }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sred[w][0] = (double)v.h + (double)v.l;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < (NT + 31) / 32; i++) s += sred[i][0];
+    return s;
+}
+
+// Last CTA of the grid: sums the first NR per-CTA partials (when `sums`) in a
+// fixed order and publishes the results.
+template <typename R, int NT, int NR>
+__device__ void finalize(const PassArgs<R>& a, double (*sred)[NRED], uint32_t nblk, bool sums) {
+    double s[NRED] = {0.0, 0.0, 0.0};
+    if (sums) {
+        double s2[NRED] = {0.0, 0.0, 0.0};  // two chains per value
+        int b = threadIdx.x;
+        for (; b + NT < (int)nblk; b += 2 * NT) {
 #pragma unroll
-    for (int r = 0; r < NRED; r++) s[r] += c[r];
-    block_sum<NT>(s, sred);
+            for (int r = 0; r < NR; r++) {
+                s[r] += __ldcg(a.partials + (size_t)b * NRED + r);
+                s2[r] += __ldcg(a.partials + (size_t)(b + NT) * NRED + r);
+            }
+        }
+        if (b < (int)nblk)
+#pragma unroll
+            for (int r = 0; r < NR; r++) s[r] += __ldcg(a.partials + (size_t)b * NRED + r);
+#pragma unroll
+        for (int r = 0; r < NR; r++) s[r] += s2[r];
+        block_sum<NT, NR>(s, sred);
+    }
     if (threadIdx.x == 0) {
         DynState* d = a.dyn;
         if (a.flags & F_FIN_S2) d->s2 = sqrt(a.npart / s[0]);
@@ -227,16 +264,31 @@ __device__ __forceinline__ void cp_async(void* dst, const void* src, int bytes) 
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
+// Columns per group of y/x pencils.  The rows of one x pencil are a whole
+// plane apart and the rows of a y pencil a whole line apart, so each row a
+// group touches should be a long contiguous run: 128 bytes for x and 64 for y
+// in the FP32 form (a copy with 32-byte rows reaches less than half the HBM
+// bandwidth of one with 128-byte rows on x pencils at 256^3 and 512^3).  The
+// FP64 form (FP64-ALU-bound) keeps 32-byte rows.  A group never exceeds the
+// CTA, so a fixed 128-thread CTA (the batched pass) narrows it.
+template <typename R, int N, int AX> __host__ __device__ constexpr int cw_target() {
+    return (sizeof(C2<R>) == 16) ? 2 : (AX == AX_X) ? 16 : 8;
+}
+template <typename R, int N, int AX, int NT> __host__ __device__ constexpr int pass_cw() {
+    constexpr int T = N / Plan<N>::E;
+    constexpr int want = ((32 / T) > cw_target<R, N, AX>()) ? (32 / T) : cw_target<R, N, AX>();
+    return (T * want <= NT) ? want : ((NT / T) > 0 ? NT / T : 1);
+}
+
 // Geometry of one pass kernel instantiation.
 //  z pencils: a warp holds 32/T whole pencils, t fastest (coalesced rows).
 //  y/x pencils: a group of G = T*CW threads holds CW adjacent columns, column
-//  fastest, so every warp-wide access covers >= 32 contiguous bytes per row.
+//  fastest, so a warp-wide access covers 32/T rows of CW contiguous points.
 template <typename R, int N, int AX, int NT>
 struct PassGeom {
     static constexpr int E = Plan<N>::E;
     static constexpr int T = N / E;
-    static constexpr int CWMIN = (sizeof(C2<R>) == 8) ? 4 : 2;
-    static constexpr int CW = (AX == AX_Z) ? (32 / T) : ((32 / T) > CWMIN ? (32 / T) : CWMIN);
+    static constexpr int CW = (AX == AX_Z) ? (32 / T) : pass_cw<R, N, AX, NT>();
     static constexpr int G = (AX == AX_Z) ? 32 : T * CW;
     static constexpr int W = NT / T;  // pencils per CTA
     static constexpr int ROW = padded_len<N>();
@@ -244,9 +296,11 @@ struct PassGeom {
     static constexpr size_t TAB_BYTES = (((size_t)(TW + N) * sizeof(C2<R>) + N * sizeof(R)) + 15) & ~(size_t)15;
     static constexpr size_t EXCH_BYTES = (size_t)W * ROW * sizeof(C2<R>);
     static constexpr size_t SMEM_BASE = TAB_BYTES + EXCH_BYTES;
-    static constexpr size_t SMEM_MAX = SMEM_BASE + 2 * (size_t)E * NT * (sizeof(C2<R>) + sizeof(R));
-    static constexpr int MINB = (sizeof(R) == 4 ? 512 : 256) / NT;
+    // the largest staged-operand set is two complex values per point (psi + V + V_qf, or lap + copy)
+    static constexpr size_t SMEM_MAX = SMEM_BASE + 2 * (size_t)E * NT * sizeof(C2<R>);
+    static constexpr int MINB = ((sizeof(R) == 4 ? 512 : 256) / NT) > 0 ? (sizeof(R) == 4 ? 512 : 256) / NT : 1;
     static_assert(NT % G == 0 && NT % 32 == 0, "threads per CTA must hold whole groups");
+    static_assert(SMEM_MAX <= 232448, "shared memory of a pass exceeds the per-CTA limit");
 };
 
 // Kernel classes: each instantiation compiles only the code its passes use,
@@ -371,6 +425,8 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     __syncthreads();  // tables staged
 
     double acc[NRED] = {0.0, 0.0, 0.0};
+    FF nff = {0.0f, 0.0f};  // FP32 form: norm partial
+    (void)nff;
 
     // The heavy pointwise ops run in rolled loops over this thread's own
     // cells of the exchange buffer (positions t + T*q, which only this thread
@@ -529,9 +585,14 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
             from_cells();
         }
         if (a.flags & F_REDUCE) {
+            if constexpr (sizeof(R) == 4) {
 #pragma unroll
-            for (int q = 0; q < E; q++)
-                acc[0] += (double)a.ph.gamma * ((double)x[q].x * (double)x[q].x + (double)x[q].y * (double)x[q].y);
+                for (int q = 0; q < E; q++) nff = ff_add(nff, a.ph.gamma * (x[q].x * x[q].x + x[q].y * x[q].y));
+            } else {
+#pragma unroll
+                for (int q = 0; q < E; q++)
+                    acc[0] += (double)a.ph.gamma * ((double)x[q].x * (double)x[q].x + (double)x[q].y * (double)x[q].y);
+            }
         }
     }
     if constexpr (CLS != C_EN) {
@@ -556,10 +617,17 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     // ------------------------------------------------- cross-CTA finalise
     if constexpr (FIN) {
         if (a.flags & (F_FIN_S2 | F_FIN_STEP | F_FIN_RED)) {
-            block_sum<NT>(acc, sred);
+            // energy: 3 sums; norm: 1; a real-time step only advances the step counter
+            constexpr int NR = (CLS == C_EN) ? 3 : 1;
+            const bool sums = (CLS == C_EN) || (a.flags & F_REDUCE);
+            if (sums) {
+                if constexpr (CLS == C_EPI && sizeof(R) == 4) acc[0] = block_sum_ff<NT>(nff, sred);
+                else block_sum<NT, NR>(acc, sred);
+            }
             if (tid == 0) {
+                if (sums)
 #pragma unroll
-                for (int r = 0; r < NRED; r++) a.partials[(size_t)blk * NRED + r] = acc[r];
+                    for (int r = 0; r < NR; r++) a.partials[(size_t)blk * NRED + r] = acc[r];
                 __threadfence();
                 const unsigned prev = atomicAdd(&a.dyn->ticket, 1u);
                 last_cta = (prev == nblk - 1);
@@ -567,7 +635,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
             __syncthreads();
             if (last_cta) {
                 __threadfence();
-                finalize<R, NT>(a, sred, nblk);
+                finalize<R, NT, NR>(a, sred, nblk, sums);
             }
         }
     }
