@@ -61,6 +61,10 @@ int gpe_gb_set_psi(gpe_gb_engine* e, double t, const double* psi);
 int gpe_gb_get_psi(gpe_gb_engine* e, double* t, double* psi);
 /* gpe_get_density (dev/gpe_engine.cu:669): density = nx*ny*nz doubles */
 int gpe_gb_get_density(gpe_gb_engine* e, double* t, double* density);
+/* gpe_get_currents (dev/gpe_engine.cu:1856-1904): probability currents
+ * j_a = Re(conj(psi) IFFT(k_a/(Gamma n) FFT psi)) along x, y, z into three
+ * host arrays of n doubles (C order). */
+int gpe_gb_get_currents(gpe_gb_engine* e, double* t, double* jx, double* jy, double* jz);
 /* gpe_get_norm (dev/gpe_engine.cu:679) */
 int gpe_gb_get_norm(gpe_gb_engine* e, double* norm);
 /* gpe_normalize_psi (dev/gpe_engine.cu:648) */

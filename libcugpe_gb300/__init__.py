@@ -39,7 +39,7 @@ ERR_NOT_IMPLEMENTED = -98
 C_ABI_SYMBOLS = [
     "gpe_gb_create", "gpe_gb_destroy", "gpe_gb_get_lattice", "gpe_gb_change_alpha_beta", "gpe_gb_set_time",
     "gpe_gb_set_user_params", "gpe_gb_set_quantum_friction_coeff", "gpe_gb_set_psi", "gpe_gb_get_psi",
-    "gpe_gb_get_density", "gpe_gb_get_norm", "gpe_gb_normalize_psi", "gpe_gb_evolve_qf", "gpe_gb_energy",
+    "gpe_gb_get_density", "gpe_gb_get_currents", "gpe_gb_get_norm", "gpe_gb_normalize_psi", "gpe_gb_evolve_qf", "gpe_gb_energy",
     "gpe_gb_set_psi_device", "gpe_gb_get_psi_device", "gpe_gb_synchronize", "gpe_gb_kernel_launches",
     "gpe_gb_use_graphs", "gpe_gb_set_potential_slices", "gpe_gb_error_string", "gpe_gb_get_stream",
     "gpe_gb_profile_passes", "gpe_gb_norm_noalloc", "gpe_gb_set_vortex", "gpe_gb_get_phase", "gpe_gb_set_phase",
@@ -81,6 +81,7 @@ def _lib():
             "gpe_gb_get_psi": (i, [vp, dp, dp]),
             "gpe_gb_get_density": (i, [vp, dp, dp]),
             "gpe_gb_get_norm": (i, [vp, dp]),
+            "gpe_gb_get_currents": (i, [vp, dp, dp, dp, dp]),
             "gpe_gb_normalize_psi": (i, [vp]),
             "gpe_gb_evolve_qf": (i, [vp, i, dp]),
             "gpe_gb_energy": (i, [vp, dp, dp, dp, dp]),
@@ -209,6 +210,14 @@ class Engine:
         t = ctypes.c_double()
         _check(_lib().gpe_gb_get_density(self._h, ctypes.byref(t), _dp(out)), "get_density")
         return t.value, out
+
+    def get_currents(self):
+        """(t, jx, jy, jz): probability currents Re(conj(psi) IFFT(k_a/(Gamma n) FFT psi))."""
+        j = [np.empty(self.shape, dtype=np.float64) for _ in range(3)]
+        t = ctypes.c_double()
+        _check(_lib().gpe_gb_get_currents(self._h, ctypes.byref(t), _dp(j[0]), _dp(j[1]), _dp(j[2])),
+               "get_currents")
+        return t.value, j[0], j[1], j[2]
 
     def get_norm(self):
         n = ctypes.c_double()

@@ -95,7 +95,10 @@ int gpe_evolve_vortex3(int nt, double* mu) { return gpe_gb_evolve_vortex(g_engin
 int gpe_evolve_enforced_phase(int nt, double* mu) { return gpe_gb_evolve_enforced_phase(g_engine, nt, mu); }
 
 // Reference entry points outside the split-step evolution of this engine.
-int gpe_get_currents(double*, double*, double*, double*) { return GPE_ERR_NOT_IMPLEMENTED; }
+int gpe_get_currents(double* t, double* jx, double* jy, double* jz) {
+    if (!g_engine) return GPE_ERR_NO_ENGINE;
+    return gpe_gb_get_currents(g_engine, t, jx, jy, jz);
+}
 int gpe_evolve_dipolar(int) { return GPE_ERR_NOT_IMPLEMENTED; }
 int gpe_evolve_dipolar(int, double*) { return GPE_ERR_NOT_IMPLEMENTED; }
 int gpe_energy_dipolar(double*, double*) { return GPE_ERR_NOT_IMPLEMENTED; }

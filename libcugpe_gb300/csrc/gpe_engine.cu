@@ -129,6 +129,11 @@ __global__ void k_from_double(const double2* in, C2<R>* out, size_t n) {
     }
 }
 
+__global__ void k_real_to_double(const float* in, double* out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = (double)in[i];
+}
+
 template <typename R>
 __global__ void k_density(const C2<R>* in, double* out, size_t n, double gamma) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
@@ -185,6 +190,7 @@ struct AxisTables {
     void* lek;    // R[N]      k^2 / (2 Gamma) / N
     void* tw;     // C2<R>[tw_len]  stage-major twiddles (gpe_fft.cuh)
     void* vt;     // R[N]      0.5 i^2 w^2, i = index - N/2
+    void* lcur;   // R[N]      k / (Gamma N)   (probability currents)
 };
 
 struct Engine {
@@ -297,7 +303,7 @@ static int upload_tables(Engine* e) {
     size_t off = 0;
     std::vector<unsigned char> host;
     size_t total = 0;
-    for (int a = 0; a < 3; a++) total += (size_t)e->n3[a] * (3 * sizeof(C2<R>) + 3 * sizeof(R)) + 256 * 5;
+    for (int a = 0; a < 3; a++) total += (size_t)e->n3[a] * (3 * sizeof(C2<R>) + 4 * sizeof(R)) + 256 * 6;
     host.assign(total, 0);
     if (!e->tabmem) GPE_CK(cudaMalloc(&e->tabmem, total));
     unsigned char* dbase = (unsigned char*)e->tabmem;
@@ -307,12 +313,13 @@ static int upload_tables(Engine* e) {
         std::vector<double> k;
         kgrid(k, N);
         const size_t okt = take(N * sizeof(C2<R>)), olq = take(N * sizeof(R)), ole = take(N * sizeof(R)),
-                     otw = take(2 * N * sizeof(C2<R>)), ovt = take(N * sizeof(R));
+                     otw = take(2 * N * sizeof(C2<R>)), ovt = take(N * sizeof(R)), ocu = take(N * sizeof(R));
         C2<R>* kt = (C2<R>*)(host.data() + okt);
         R* lq = (R*)(host.data() + olq);
         R* le = (R*)(host.data() + ole);
         C2<R>* tw = (C2<R>*)(host.data() + otw);
         R* vt = (R*)(host.data() + ovt);
+        R* cu = (R*)(host.data() + ocu);
         const double w = e->up[a];
         for (int i = 0; i < N; i++) {
             // exp(c3 k^2 / Gamma^2) (dev/gpe_engine.cu:186-216), with 1/N_a of the unnormalised inverse
@@ -326,10 +333,11 @@ static int upload_tables(Engine* e) {
             le[i] = (R)((k[i] * k[i]) / (2.0 * e->gamma) / (double)N);
             const double ii = (double)i - 1.0 * (N / 2);
             vt[i] = (R)(0.5 * ii * ii * w * w);  // dev/gpe_user_defined.h:500-510
+            cu[i] = (R)(k[i] / (e->gamma * (double)N));  // dev/gpe_engine.cu:1826 with 1/N_a of the inverse
         }
         e->ax[a].ktab = dbase + okt; e->ax[a].lqf = dbase + olq; e->ax[a].lek = dbase + ole;
         stage_twiddles<R>(N, tw);
-        e->ax[a].tw = dbase + otw; e->ax[a].vt = dbase + ovt;
+        e->ax[a].tw = dbase + otw; e->ax[a].vt = dbase + ovt; e->ax[a].lcur = dbase + ocu;
     }
     GPE_CK(cudaMemcpyAsync(e->tabmem, host.data(), off, cudaMemcpyHostToDevice, e->st));
     GPE_CK(cudaStreamSynchronize(e->st));
@@ -463,6 +471,14 @@ static PassArgs<R> desc_args(const Engine* e, const PassDesc& d) {
 template <typename R>
 static int launch_desc(Engine* e, const PassDesc& d) {
     const PassArgs<R> a = desc_args<R>(e, d);
+    e->launches++;
+    return cuda_rc(launch_pass<R>(a, e->n3[d.axis], d.axis, pencils_of(e, d.axis), e->st));
+}
+
+template <typename R>
+static int launch_current(Engine* e, const PassDesc& d) {
+    PassArgs<R> a = desc_args<R>(e, d);
+    a.ltab = (const R*)e->ax[d.axis].lcur;
     e->launches++;
     return cuda_rc(launch_pass<R>(a, e->n3[d.axis], d.axis, pencils_of(e, d.axis), e->st));
 }
@@ -1409,6 +1425,32 @@ int gpe_gb_get_density(gpe_gb_engine* h, double* t, double* density) {
     GPE_CK(cudaGetLastError());
     GPE_CK(cudaMemcpyAsync(density, e->dens, sizeof(double) * e->n, cudaMemcpyDeviceToHost, e->st));
     GPE_CK(cudaStreamSynchronize(e->st));
+    if (t) *t = e->t0 + e->dt * e->it;
+    return 0;
+}
+
+int gpe_gb_get_currents(gpe_gb_engine* h, double* t, double* jx, double* jy, double* jz) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    if (!jx || !jy || !jz) return GPE_ERR_ARGUMENT;
+    Engine* e = &h->e;
+    double* out[3] = {jx, jy, jz};
+    if (e->prec == GPE_PRECISION_FP32 && !e->dens) GPE_CK(cudaMalloc(&e->dens, sizeof(double) * e->n));
+    for (int a = 0; a < 3; a++) {
+        // one axis pass: FFT_a, x k_a/(Gamma N_a), inverse FFT_a, Re(conj(psi) .) -> V (scratch between steps)
+        const gpe::PassDesc d = {a, gpe::PRE_NONE, gpe::MID_CURRENT, gpe::POST_NONE, gpe::F_LAP, gpe::B_PSI, gpe::B_NONE};
+        GPE_RC(e->prec == GPE_PRECISION_FP32 ? gpe::launch_current<float>(e, d) : gpe::launch_current<double>(e, d));
+        if (e->prec == GPE_PRECISION_FP32) {
+            int b, th;
+            gpe::util_grid(e->n, &b, &th);
+            gpe::k_real_to_double<<<b, th, 0, e->st>>>((const float*)e->V, e->dens, e->n);
+            e->launches++;
+            GPE_CK(cudaGetLastError());
+            GPE_CK(cudaMemcpyAsync(out[a], e->dens, sizeof(double) * e->n, cudaMemcpyDeviceToHost, e->st));
+        } else {
+            GPE_CK(cudaMemcpyAsync(out[a], e->V, sizeof(double) * e->n, cudaMemcpyDeviceToHost, e->st));
+        }
+        GPE_CK(cudaStreamSynchronize(e->st));
+    }
     if (t) *t = e->t0 + e->dt * e->it;
     return 0;
 }

@@ -36,6 +36,7 @@ enum : int {  // MID ops (after the Laplacian pair)
     MID_LAP_STORE = 1,  // lap = D_a psi
     MID_LAP_ACC = 2,    // lap += D_a psi
     MID_QF_VSTEP1 = 3,  // V_qf from lap + D_a psi, then Vstep1_qf         (:744-768, 907-918)
+    MID_CURRENT = 4,    // V = Re(conj(psi) D_a psi), D_a = k_a/(Gamma N_a)  (:1817-1904)
 };
 enum : int {  // POST ops
     POST_NONE = 0,
@@ -236,6 +237,7 @@ __host__ __device__ inline uint32_t staged_ops(int mid, int post, uint32_t flags
     uint32_t m = 0;
     if (mid == MID_LAP_ACC) m |= OP_LAP;
     if (mid == MID_QF_VSTEP1) m |= OP_LAP | OP_COPY;
+    if (mid == MID_CURRENT) m |= OP_COPY;
     if (post == POST_VSTEP2 || post == POST_PART12) m |= OP_PSI | OP_V;
     if (post == POST_PART12 && (flags & F_QF)) m |= OP_VQF;
     if (post == POST_PART1) m |= OP_V;
@@ -534,6 +536,14 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                     own(q) = cmul(p, phase(a.ph, V));
                 }
                 from_cells();
+            } else if (a.mid == MID_CURRENT) {
+                // probability current along the pass axis: Re(conj(psi) IFFT(k_a/(Gamma N_a) FFT psi))
+                // (cplxMulR of dev/gpe_engine.cu:1660-1667 after the k_a multiply of :1817-1854)
+#pragma unroll
+                for (int q = 0; q < E; q++) {
+                    const C2<R> p = slotB[q * NT + tid];
+                    a.V[at(q)] = p.x * x[q].x + p.y * x[q].y;
+                }
             }
         }
     }

@@ -70,6 +70,8 @@ def lib():
         L.oracle_evolve_qf.restype = i
         L.oracle_energy.argtypes = [vp, dp, dp, dp, dp]
         L.oracle_energy.restype = i
+        L.oracle_get_currents.argtypes = [vp, dp, dp, dp, dp]
+        L.oracle_get_currents.restype = i
         L.oracle_fft3d.argtypes = [i, i, i, dp, i, i]
         L.oracle_set_vortex.argtypes = [vp, d, d, i]
         L.oracle_get_phase.argtypes = [vp, dp]
@@ -139,6 +141,13 @@ class Oracle:
         t = ctypes.c_double()
         lib().oracle_get_density(self._h, ctypes.byref(t), _dp(out))
         return t.value, out
+
+    def get_currents(self):
+        """(t, jx, jy, jz) as gpe_get_currents (dev/gpe_engine.cu:1856-1904)."""
+        j = [np.empty(self.shape, dtype=np.float64) for _ in range(3)]
+        t = ctypes.c_double()
+        lib().oracle_get_currents(self._h, ctypes.byref(t), _dp(j[0]), _dp(j[1]), _dp(j[2]))
+        return t.value, j[0], j[1], j[2]
 
     def get_norm(self):
         return lib().oracle_get_norm(self._h)

@@ -562,6 +562,32 @@ int oracle_energy(void *h, double *t, double *ekin, double *eint, double *eext) 
     return 0;
 }
 
+int oracle_get_currents(void *h, double *t, double *jx, double *jy, double *jz) {
+    /* dev/gpe_engine.cu:1856-1904: psi2 = FFT psi; per axis a: IFFT(k_a/(Gamma n) psi2),
+     * j_a = Re(conj(psi) .) (cplxMulR, :1660-1667) */
+    gpe_oracle *o = (gpe_oracle *)h;
+    const int ny = o->ny, nz = o->nz;
+    const long n = (long)o->n;
+    *t = o->t0 + o->dt * o->it;
+    memcpy(o->psi2, o->psi, sizeof(cd) * o->n);
+    fft3d(o, o->psi2, -1);
+    double *out[3] = {jx, jy, jz};
+    const double *ks[3] = {o->kx, o->ky, o->kz};
+    const double den = o->gamma * (double)o->n;
+    for (int a = 0; a < 3; a++) {
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+        for (long i = 0; i < n; i++) {
+            DECODE((size_t)i);
+            const int ia = (a == 0) ? ix : (a == 1) ? iy : iz;
+            o->wrk3C[i] = cscale(o->psi2[i], ks[a][ia] / den);
+        }
+        fft3d(o, o->wrk3C, +1);
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+        for (long i = 0; i < n; i++) out[a][i] = o->psi[i].x * o->wrk3C[i].x + o->psi[i].y * o->wrk3C[i].y;
+    }
+    return 0;
+}
+
 /* raw 3D transform, exposed so the tests can pin the restated FFT against numpy */
 void oracle_fft3d(int nx, int ny, int nz, double *a, int sign, int nthreads) {
     gpe_oracle o;

@@ -35,7 +35,7 @@ def run(shape, interactions, alpha, beta, dt, npart, params, psi0, cmds, qf=0.0,
         r = subprocess.run(args, capture_output=True, text=True, timeout=timeout)
         if r.returncode != 0:
             raise RuntimeError(f"reference run failed ({r.returncode}): {r.stderr[-2000:]}")
-        out = {"psi": [], "energy": [], "mu": [], "time_ms": [], "t": []}
+        out = {"psi": [], "energy": [], "mu": [], "time_ms": [], "t": [], "currents": []}
         for line in r.stdout.splitlines():
             f = line.split()
             if not f:
@@ -51,5 +51,10 @@ def run(shape, interactions, alpha, beta, dt, npart, params, psi0, cmds, qf=0.0,
         k = 0
         while os.path.isfile(os.path.join(d, f"psi_{k}.bin")):
             out["psi"].append(np.fromfile(os.path.join(d, f"psi_{k}.bin"), dtype=np.complex128).reshape(shape))
+            k += 1
+        k = 0
+        while os.path.isfile(os.path.join(d, f"cur_{k}.bin")):
+            j = np.fromfile(os.path.join(d, f"cur_{k}.bin"), dtype=np.float64).reshape((3,) + tuple(shape))
+            out["currents"].append((j[0], j[1], j[2]))
             k += 1
         return out

@@ -21,6 +21,7 @@
 //     V<m>_<k>  gpe_evolve_vortex (m=1), _vortex2 (2), _vortex3 (3), k steps -> "MU mu"
 //     G      gpe_get_phase(NULL)
 //     P<k>   gpe_evolve_enforced_phase(k, &mu) -> "MU mu"
+//     J      gpe_get_currents() -> OUTDIR/cur_<i>.bin (jx, jy, jz), "J t"
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -52,7 +53,7 @@ int main(int argc, char** argv) {
     if (qf != 0.0) CHECK(gpe_set_quantum_friction_coeff(qf));
     CHECK(gpe_set_psi(0.0, psi.data()));
 
-    int dump = 0;
+    int dump = 0, currents = 0;
     size_t pos = 0;
     while (pos < cmds.size()) {
         size_t end = cmds.find(',', pos);
@@ -109,6 +110,17 @@ int main(int argc, char** argv) {
             else if (m == 2) CHECK(gpe_evolve_vortex2(k, &mu));
             else CHECK(gpe_evolve_vortex3(k, &mu));
             printf("MU %.17g\n", mu);
+        } else if (c == "J") {
+            double t;
+            std::vector<double> j(3 * n);
+            CHECK(gpe_get_currents(&t, j.data(), j.data() + n, j.data() + 2 * n));
+            char name[64];
+            snprintf(name, sizeof name, "/cur_%d.bin", currents++);
+            FILE* g = fopen((outdir + name).c_str(), "wb");
+            if (!g) { fprintf(stderr, "cannot write\n"); return 1; }
+            fwrite(j.data(), sizeof(double), 3 * n, g);
+            fclose(g);
+            printf("J %.17g\n", t);
         } else if (c == "G") {
             CHECK(gpe_get_phase(NULL));
         } else if (c[0] == 'P') {

@@ -195,3 +195,29 @@ def test_phase_enforcing_evolves_match_oracle(cuda_device, gpe_lib, case, method
     if CASES[case][2] != 0.0:
         assert abs(mu_e - mu_o) <= 1e-10 * max(1.0, abs(mu_o))
     np.testing.assert_allclose(e.get_phase(), o.get_phase(), atol=1e-9)
+
+
+@pytest.mark.parametrize("shape", [(16, 16, 16), (32, 16, 8), (8, 256, 8), (512, 8, 16)])
+def test_currents_match_oracle(cuda_device, gpe_lib, shape):
+    """gpe_get_currents: one axis pass per component (FFT_a, x k_a/(Gamma N_a), inverse,
+    Re(conj(psi) .)) against the oracle's 3D-FFT restatement; FP64 <= 1e-12, FP32 <= 5e-5 (the
+    currents of a random-phase state are small differences of large products)."""
+    e, o, _ = make_pair(shape, "ufg_rte_qf")
+    o.evolve_qf(3)
+    t, p = o.get_psi()
+    e.set_psi(t, p)
+    o.set_psi(t, p)
+    ref = o.get_currents()
+    got = e.get_currents()
+    assert got[0] == pytest.approx(ref[0])
+    for a in range(1, 4):
+        assert rel(got[a], ref[a]) <= 1e-12, (a, rel(got[a], ref[a]))
+    # currents leave the evolution untouched: the next steps still match
+    e.evolve_qf(2)
+    o.evolve_qf(2)
+    assert rel(e.get_psi()[1], o.get_psi()[1]) <= 5e-12
+    e32, o32, _ = make_pair(shape, "bec_rte", precision=g.FP32)
+    ref = o32.get_currents()
+    got = e32.get_currents()
+    for a in range(1, 4):
+        assert rel(got[a], ref[a]) <= 5e-5, (a, rel(got[a], ref[a]))

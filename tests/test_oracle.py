@@ -167,3 +167,27 @@ def test_vortex_imprint_keeps_winding_through_ite():
     for (a, b), (c, d) in zip(loop, loop[1:] + loop[:1]):
         w += (ph[c, d] - ph[a, b] + np.pi) % (2 * np.pi) - np.pi
     assert abs(abs(w) - 2 * np.pi) < 1e-6
+
+
+def test_oracle_currents_plane_wave_and_numpy():
+    """gpe_get_currents (dev/gpe_engine.cu:1856-1904): a plane wave e^{i k0 x} carries
+    j_x = |A|^2 k0 / Gamma; a random state matches a numpy restatement."""
+    shape = (16, 8, 32)
+    gamma = 2.0
+    ix = np.arange(shape[0])[:, None, None]
+    k0 = 2 * np.pi * 3 / shape[0]
+    psi = 0.7 * np.exp(1j * k0 * ix) * np.ones(shape)
+    o = oracle.Oracle(shape, 0, 1.0, 0.0, 0.05, 1000.0, threads=2)
+    o.set_psi(0.0, psi)
+    _, jx, jy, jz = o.get_currents()
+    assert np.allclose(jx, 0.49 * k0 / gamma, rtol=1e-13, atol=1e-14)
+    assert np.max(np.abs(jy)) < 1e-14 and np.max(np.abs(jz)) < 1e-14
+    psi = configs.random_state(shape, seed=9, npart=1000.0, gamma=gamma)
+    o.set_psi(0.0, psi)
+    _, jx, jy, jz = o.get_currents()
+    f = np.fft.fftn(psi)
+    for a, j in enumerate((jx, jy, jz)):
+        # numpy's grid, like the reference's (dev/gpe_engine.cu:147-154), puts -pi at n/2
+        kk = (2 * np.pi * np.fft.fftfreq(shape[a])).reshape([-1 if b == a else 1 for b in range(3)])
+        ref = np.real(np.conj(psi) * np.fft.ifftn(kk / gamma * f))
+        assert rel(j, ref) < 1e-13, a

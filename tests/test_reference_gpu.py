@@ -128,3 +128,16 @@ def test_phase_enforcing_evolves_match_reference(reference, gpe_lib, beta, metho
     assert rel(ours, out["psi"][0]) <= 3e-12, rel(ours, out["psi"][0])
     if beta != 0.0:
         assert abs(mu - out["mu"][0]) <= 1e-10 * max(1.0, abs(out["mu"][0]))
+
+
+@pytest.mark.parametrize("case", [CASES[0], CASES[3]], ids=["bec", "ufg_qf"])
+def test_currents_match_reference(reference, gpe_lib, case):
+    """gpe_get_currents against the reference's own on the reference's state after 3 RTE steps."""
+    shape, inter, alpha, beta, dt, npart, params, qf = case
+    gamma = 1.0 if inter == -1 else 2.0
+    psi = configs.random_state(shape, seed=24, npart=npart, gamma=gamma)
+    out = ref_run.run(shape, inter, 1.0, 0.0, dt, npart, params, psi, ["S3", "J", "D"], qf=qf)
+    e = engine_for(shape, inter, 1.0, 0.0, dt, npart, params, qf, out["psi"][0])
+    _, jx, jy, jz = e.get_currents()
+    for ours, ref in zip((jx, jy, jz), out["currents"][0]):
+        assert rel(ours, ref) <= 1e-12, rel(ours, ref)
