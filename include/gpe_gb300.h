@@ -30,6 +30,7 @@ extern "C" {
 #define GPE_ERR_ARGUMENT (-12)         /* null pointer or bad value */
 #define GPE_ERR_FUNCTIONAL (-13)       /* unknown interactions code */
 #define GPE_ERR_NOALLOC_SIZE (-14)     /* more points than gpe_gb_norm_noalloc's scratch serves */
+#define GPE_ERR_IO (-15)               /* a .dftc / .dftc.info file could not be opened, read or written */
 #define GPE_ERR_NOT_IMPLEMENTED (-98)  /* reference entry point outside this engine */
 
 #define GPE_PRECISION_FP64 0 /* plain FP64 drop-in */
@@ -176,6 +177,30 @@ int gpe_gb_control_loss(gpe_gb_control* c, const double* controls, const double*
 int gpe_gb_control_loss_grad(gpe_gb_control* c, const double* controls, const double* psi0, double* loss,
                              double* grad);
 int gpe_gb_control_destroy(gpe_gb_control* c);
+/* Snapshots in the .dftc format (dev/gpe_io.h:45-166; frames as in
+ * test_vortex/rte_vortex.c:64-90 with the queue of dev/gpe_queue.h:67-137).
+ * open: creates `dftc_path` and nbuf (1..64) device + pinned frame buffers
+ * of nx*ny*nz complex128 each, and a writer thread.  push: copies psi on the
+ * engine's stream into a free frame buffer (waits while all nbuf are in
+ * flight), returns with the engine free to evolve while the frame goes to
+ * the host on a side stream and is appended to the file; *t = its time.
+ * close: waits for every pushed frame, closes the file, frees everything;
+ * *frames = frames written.  One pipeline per engine at a time. */
+typedef struct gpe_gb_snapshots gpe_gb_snapshots;
+int gpe_gb_snapshots_open(gpe_gb_snapshots** out, gpe_gb_engine* e, const char* dftc_path, int nbuf);
+int gpe_gb_snapshots_push(gpe_gb_snapshots* s, double* t);
+int gpe_gb_snapshots_close(gpe_gb_snapshots* s, long long* frames);
+/* gpe_save_info (dev/gpe_io.h:45-104): writes `<dftc_path>.info`; system is
+ * "bosons" or "fermions", mode "contact", "dipolar", "unitary" or "bec". */
+int gpe_gb_dftc_write_info(const char* dftc_path, const char* system, const char* mode, int nx, int ny, int nz,
+                           double dt, int nom, double a_scat, double aspect_ratio, double omega_x, double r0,
+                           double npart, double total_time);
+/* gpe_get_info (dev/gpe_io.h:130-166): reads `<dftc_path>.info`; system and
+ * mode (may be NULL) receive the first word of their lines, at most len-1
+ * characters; total_time (may be NULL) is 0 when the file has no such line. */
+int gpe_gb_dftc_read_info(const char* dftc_path, char* system, char* mode, int len, int* nx, int* ny, int* nz,
+                          double* dt, int* nom, double* a_scat, double* aspect_ratio, double* omega_x, double* r0,
+                          double* npart, double* total_time);
 /* Message for a return code. */
 const char* gpe_gb_error_string(int code);
 

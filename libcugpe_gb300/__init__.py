@@ -33,6 +33,7 @@ ERR_NO_ENGINE = -11
 ERR_ARGUMENT = -12
 ERR_FUNCTIONAL = -13
 ERR_NOALLOC_SIZE = -14
+ERR_IO = -15
 ERR_NOT_IMPLEMENTED = -98
 
 # entry points declared in include/gpe_gb300.h
@@ -46,7 +47,8 @@ C_ABI_SYMBOLS = [
     "gpe_gb_evolve_vortex", "gpe_gb_evolve_enforced_phase", "gpe_gb_batch_create", "gpe_gb_batch_destroy",
     "gpe_gb_batch_engine", "gpe_gb_batch_set_active", "gpe_gb_batch_evolve", "gpe_gb_batch_chemical_potentials",
     "gpe_gb_batch_kernel_launches", "gpe_gb_chemical_potential", "gpe_gb_control_create", "gpe_gb_control_loss",
-    "gpe_gb_control_loss_grad", "gpe_gb_control_destroy",
+    "gpe_gb_control_loss_grad", "gpe_gb_control_destroy", "gpe_gb_snapshots_open", "gpe_gb_snapshots_push",
+    "gpe_gb_snapshots_close", "gpe_gb_dftc_write_info", "gpe_gb_dftc_read_info",
 ]
 
 
@@ -112,6 +114,13 @@ def _lib():
             "gpe_gb_control_loss_grad": (i, [vp, dp, dp, dp, dp]),
             "gpe_gb_control_destroy": (i, [vp]),
             "gpe_gb_profile_passes": (i, [vp, i, ctypes.POINTER(ctypes.c_float), dp, ip, ip, i, ip]),
+            "gpe_gb_snapshots_open": (i, [ctypes.POINTER(vp), vp, ctypes.c_char_p, i]),
+            "gpe_gb_snapshots_push": (i, [vp, dp]),
+            "gpe_gb_snapshots_close": (i, [vp, ctypes.POINTER(ctypes.c_longlong)]),
+            "gpe_gb_dftc_write_info": (i, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, i, i, i, d, i, d, d,
+                                           d, d, d, d]),
+            "gpe_gb_dftc_read_info": (i, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, i, ip, ip, ip, dp, ip,
+                                          dp, dp, dp, dp, dp, dp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)

@@ -43,6 +43,7 @@ def _sources():
     units.append(os.path.join(CSRC, "gpe_noalloc.cu"))
     units.append(os.path.join(CSRC, "gpe_batch_kernels.cu"))
     units.append(os.path.join(CSRC, "gpe_dropin.cpp"))
+    units.append(os.path.join(CSRC, "gpe_snapshots.cpp"))
     return units
 
 

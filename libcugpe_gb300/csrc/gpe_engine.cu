@@ -1797,6 +1797,7 @@ const char* gpe_gb_error_string(int code) {
         case GPE_ERR_FUNCTIONAL: return "unknown interactions code";
         case GPE_ERR_NOT_IMPLEMENTED: return "entry point not implemented by this engine";
         case GPE_ERR_NOALLOC_SIZE: return "more points than the allocation-free scratch serves (max 2^27)";
+        case GPE_ERR_IO: return "a .dftc or .dftc.info file could not be opened, read or written";
         default: break;
     }
     if (code > 0) return cudaGetErrorString((cudaError_t)code);
