@@ -56,6 +56,15 @@ int gpe_gb_set_time(gpe_gb_engine* e, double t0);
 int gpe_gb_set_user_params(gpe_gb_engine* e, int size, const double* params);
 /* gpe_set_quantum_friction_coeff (dev/gpe_engine.cu:435) */
 int gpe_gb_set_quantum_friction_coeff(gpe_gb_engine* e, double qfcoeff);
+/* Weizsaecker gradient term of weight lambda (no reference counterpart: the
+ * reference declares gpe_gradient_corrections, dev/gpe_user_defined.h:158,
+ * but never calls it).  Adds E_W = (lambda/8) sum |grad rho|^2 / rho to the
+ * functional, i.e. V_W = (lambda/8) (|grad rho|^2/rho^2 - 2 lap(rho)/rho)
+ * (lattice units, hbar = m = 1, rho = Gamma |psi|^2, rho regularised by
+ * +1e-12), with spectral derivatives of psi.  Like the friction potential,
+ * V_W is evaluated once per step at the step's initial psi and enters both
+ * halves of the step.  0 turns it off.  FP32 form: x side <= 256. */
+int gpe_gb_set_weizsacker(gpe_gb_engine* e, double lambda);
 /* gpe_set_psi (dev/gpe_engine.cu:694): psi = 2*nx*ny*nz doubles */
 int gpe_gb_set_psi(gpe_gb_engine* e, double t, const double* psi);
 /* gpe_get_psi (dev/gpe_engine.cu:705) */

@@ -48,7 +48,7 @@ C_ABI_SYMBOLS = [
     "gpe_gb_batch_engine", "gpe_gb_batch_set_active", "gpe_gb_batch_evolve", "gpe_gb_batch_chemical_potentials",
     "gpe_gb_batch_kernel_launches", "gpe_gb_chemical_potential", "gpe_gb_control_create", "gpe_gb_control_loss",
     "gpe_gb_control_loss_grad", "gpe_gb_control_destroy", "gpe_gb_snapshots_open", "gpe_gb_snapshots_push",
-    "gpe_gb_snapshots_close", "gpe_gb_dftc_write_info", "gpe_gb_dftc_read_info",
+    "gpe_gb_snapshots_close", "gpe_gb_dftc_write_info", "gpe_gb_dftc_read_info", "gpe_gb_set_weizsacker",
 ]
 
 
@@ -79,6 +79,7 @@ def _lib():
             "gpe_gb_set_time": (i, [vp, d]),
             "gpe_gb_set_user_params": (i, [vp, i, dp]),
             "gpe_gb_set_quantum_friction_coeff": (i, [vp, d]),
+            "gpe_gb_set_weizsacker": (i, [vp, d]),
             "gpe_gb_set_psi": (i, [vp, d, dp]),
             "gpe_gb_get_psi": (i, [vp, dp, dp]),
             "gpe_gb_get_density": (i, [vp, dp, dp]),
@@ -195,6 +196,10 @@ class Engine:
 
     def set_quantum_friction_coeff(self, q):
         _check(_lib().gpe_gb_set_quantum_friction_coeff(self._h, float(q)), "set_quantum_friction_coeff")
+
+    def set_weizsacker(self, lam):
+        """Weizsaecker gradient term (lambda/8) |grad rho|^2/rho in the functional; 0 turns it off."""
+        _check(_lib().gpe_gb_set_weizsacker(self._h, float(lam)), "set_weizsacker")
 
     def set_psi(self, t, psi):
         p = np.ascontiguousarray(psi, dtype=np.complex128).reshape(self.shape)

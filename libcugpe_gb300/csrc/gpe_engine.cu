@@ -186,11 +186,12 @@ __global__ void __launch_bounds__(kRedThreads) k_norm(const C2<R>* in, size_t n,
 
 struct AxisTables {
     void* ktab;   // C2<R>[N]  exp(c3 k^2 / Gamma^2) / N
-    void* lqf;    // R[N]      (qf / Gamma) k^2 / N
+    void* lqf;    // R[N]      k^2 / N   (second derivative; friction and Weizsaecker terms)
     void* lek;    // R[N]      k^2 / (2 Gamma) / N
     void* tw;     // C2<R>[tw_len]  stage-major twiddles (gpe_fft.cuh)
     void* vt;     // R[N]      0.5 i^2 w^2, i = index - N/2
     void* lcur;   // R[N]      k / (Gamma N)   (probability currents)
+    void* ld1;    // R[N]      k / N           (first derivative, Weizsaecker term)
 };
 
 struct Engine {
@@ -201,11 +202,13 @@ struct Engine {
     double gamma = 1.0;
     int prec = GPE_PRECISION_FP64;
     double alpha = 0, beta = 0, dt = 0, npart = 1, t0 = 0, qf_raw = 0;
+    double wz = 0;  // Weizsaecker weight lambda (0: off)
     unsigned it = 0;
     double up[32] = {0};
     cudaStream_t st = nullptr;
 
     void *psi = nullptr, *psi2 = nullptr, *lap = nullptr, *aux = nullptr, *V = nullptr, *Vqf = nullptr;
+    void *wg = nullptr, *ws = nullptr;  // Weizsaecker gradient sums (R[n] each)
     DynState* dyn = nullptr;
     double* partials = nullptr;
     void* tabmem = nullptr;
@@ -229,6 +232,8 @@ struct Engine {
     long long launches = 0;
 
     size_t rsize() const { return prec == GPE_PRECISION_FP32 ? sizeof(float) : sizeof(double); }
+    // friction or Weizsaecker term on: the step runs the gradient schedule
+    bool grad_terms() const { return qf_raw != 0.0 || wz != 0.0; }
     size_t csize() const { return 2 * rsize(); }
 };
 
@@ -303,7 +308,7 @@ static int upload_tables(Engine* e) {
     size_t off = 0;
     std::vector<unsigned char> host;
     size_t total = 0;
-    for (int a = 0; a < 3; a++) total += (size_t)e->n3[a] * (3 * sizeof(C2<R>) + 4 * sizeof(R)) + 256 * 6;
+    for (int a = 0; a < 3; a++) total += (size_t)e->n3[a] * (3 * sizeof(C2<R>) + 5 * sizeof(R)) + 256 * 7;
     host.assign(total, 0);
     if (!e->tabmem) GPE_CK(cudaMalloc(&e->tabmem, total));
     unsigned char* dbase = (unsigned char*)e->tabmem;
@@ -313,13 +318,15 @@ static int upload_tables(Engine* e) {
         std::vector<double> k;
         kgrid(k, N);
         const size_t okt = take(N * sizeof(C2<R>)), olq = take(N * sizeof(R)), ole = take(N * sizeof(R)),
-                     otw = take(2 * N * sizeof(C2<R>)), ovt = take(N * sizeof(R)), ocu = take(N * sizeof(R));
+                     otw = take(2 * N * sizeof(C2<R>)), ovt = take(N * sizeof(R)), ocu = take(N * sizeof(R)),
+                     od1 = take(N * sizeof(R));
         C2<R>* kt = (C2<R>*)(host.data() + okt);
         R* lq = (R*)(host.data() + olq);
         R* le = (R*)(host.data() + ole);
         C2<R>* tw = (C2<R>*)(host.data() + otw);
         R* vt = (R*)(host.data() + ovt);
         R* cu = (R*)(host.data() + ocu);
+        R* d1 = (R*)(host.data() + od1);
         const double w = e->up[a];
         for (int i = 0; i < N; i++) {
             // exp(c3 k^2 / Gamma^2) (dev/gpe_engine.cu:186-216), with 1/N_a of the unnormalised inverse
@@ -329,15 +336,17 @@ static int upload_tables(Engine* e) {
             const double ex = exp(zx);
             kt[i].x = (R)(ex * cos(zy) / (double)N);
             kt[i].y = (R)(ex * sin(zy) / (double)N);
-            lq[i] = (R)((e->qf_raw / e->gamma) * (k[i] * k[i]) / (double)N);
+            lq[i] = (R)((k[i] * k[i]) / (double)N);
             le[i] = (R)((k[i] * k[i]) / (2.0 * e->gamma) / (double)N);
             const double ii = (double)i - 1.0 * (N / 2);
             vt[i] = (R)(0.5 * ii * ii * w * w);  // dev/gpe_user_defined.h:500-510
             cu[i] = (R)(k[i] / (e->gamma * (double)N));  // dev/gpe_engine.cu:1826 with 1/N_a of the inverse
+            d1[i] = (R)(k[i] / (double)N);
         }
         e->ax[a].ktab = dbase + okt; e->ax[a].lqf = dbase + olq; e->ax[a].lek = dbase + ole;
         stage_twiddles<R>(N, tw);
         e->ax[a].tw = dbase + otw; e->ax[a].vt = dbase + ovt; e->ax[a].lcur = dbase + ocu;
+        e->ax[a].ld1 = dbase + od1;
     }
     GPE_CK(cudaMemcpyAsync(e->tabmem, host.data(), off, cudaMemcpyHostToDevice, e->st));
     GPE_CK(cudaStreamSynchronize(e->st));
@@ -363,6 +372,8 @@ static Phys<R> make_phys(const Engine* e) {
     p.c_bec = (R)(4 * M_PI * e->up[3]);
     p.a_scat = (R)e->up[3];
     p.qf_eps = (R)1.0e-12;
+    p.qf_g = (R)(e->qf_raw / e->gamma);
+    p.wz8 = (R)(e->wz / 8.0);
     return p;
 }
 
@@ -378,7 +389,7 @@ enum { B_NONE = 0, B_PSI = 1, B_PSI2 = 2 };
 static std::vector<PassDesc> schedule(const Engine* e, bool first) {
     std::vector<PassDesc> s;
     const bool ite = e->beta != 0.0;
-    const bool qf = e->qf_raw != 0.0;
+    const bool qf = e->grad_terms();
     const uint32_t aux = (e->prec == GPE_PRECISION_FP64) ? F_AUX_CPLX : 0u;
     const uint32_t sin_ = ite ? F_SCALE_IN : 0u;
     if (!qf) {
@@ -419,6 +430,12 @@ static std::vector<PassDesc> schedule(const Engine* e, bool first) {
                          F_KIN | F_STORE | aux | F_REDUCE | F_FIN_STEP | F_LAP_OUT, B_PSI, B_PSI});
         }
     }
+    if (qf && e->wz != 0.0) {
+        // the passes that take the derivatives of psi also gather the Weizsaecker sums
+        for (PassDesc& d : s)
+            if (d.mid == MID_LAP_STORE || d.mid == MID_LAP_ACC || d.mid == MID_QF_VSTEP1 || (d.flags & F_LAP_OUT))
+                d.flags |= F_WZ;
+    }
     return s;
 }
 
@@ -432,6 +449,8 @@ static PassArgs<R> base_args(const Engine* e) {
     a.aux = e->aux;
     a.V = (R*)e->V;
     a.Vqf = (R*)e->Vqf;
+    a.wg = (R*)e->wg;
+    a.ws = (R*)e->ws;
     a.vx = (const R*)e->ax[0].vt;
     a.vy = (const R*)e->ax[1].vt;
     a.vz = (const R*)e->ax[2].vt;
@@ -451,6 +470,7 @@ template <typename R>
 static void axis_args(const Engine* e, PassArgs<R>& a, int axis) {
     a.ktab = (const C2<R>*)e->ax[axis].ktab;
     a.tw = (const C2<R>*)e->ax[axis].tw;
+    a.ld1 = (const R*)e->ax[axis].ld1;
 }
 
 static size_t pencils_of(const Engine* e, int axis) { return e->n / (size_t)e->n3[axis]; }
@@ -520,7 +540,7 @@ static int finish_ite(Engine* e);
 // Runs `nsteps` steady steps directly with CUDA events around every pass.
 static int profile_passes(Engine* e, int nsteps, float* ms, double* bytes, int* axis, int* cls, int cap,
                           int* npass) {
-    if (e->qf_raw != 0.0 && !e->lap_valid) {
+    if (e->grad_terms() && !e->lap_valid) {
         GPE_RC(run_steps(e, schedule(e, true), 1));
         e->it += 1;
         e->lap_valid = true;
@@ -603,7 +623,7 @@ static const int kGraphSteps = 16;
 
 static int evolve(Engine* e, int nt, double* mu) {
     if (nt <= 0) return 0;
-    const bool qf = e->qf_raw != 0.0;
+    const bool qf = e->grad_terms();
     const std::vector<PassDesc> s = schedule(e, false);
     e->passes_per_step = (int)s.size();
     int done = 0;
@@ -738,6 +758,7 @@ static size_t max_grid(const Engine* e) {
 static void release(Engine* e) {
     drop_graph(e);
     cudaFree(e->psi); cudaFree(e->psi2); cudaFree(e->lap); cudaFree(e->aux); cudaFree(e->V); cudaFree(e->Vqf);
+    cudaFree(e->wg); cudaFree(e->ws);
     cudaFree(e->dyn); cudaFree(e->partials); cudaFree(e->tabmem); cudaFree(e->stage); cudaFree(e->dens);
     cudaFree(e->vextra);
     cudaFree(e->phase);
@@ -1202,7 +1223,7 @@ static int batch_evolve(gpe_gb_batch* b, int nt) {
     for (size_t i = 0; i < b->eng.size(); i++) {
         Engine* e = &b->eng[i]->e;
         if (!b->active[i]) continue;
-        if (e->qf_raw != 0.0 || e->prec != GPE_PRECISION_FP32) return GPE_ERR_ARGUMENT;
+        if (e->grad_terms() || e->prec != GPE_PRECISION_FP32) return GPE_ERR_ARGUMENT;
         if (e->version != b->built_version[i]) stale = true;
     }
     if (stale) GPE_RC(batch_build(b));
@@ -1331,20 +1352,42 @@ int gpe_gb_set_user_params(gpe_gb_engine* h, int size, const double* params) {
     return gpe::upload(&h->e);
 }
 
-int gpe_gb_set_quantum_friction_coeff(gpe_gb_engine* h, double q) {
-    if (!h) return GPE_ERR_NO_ENGINE;
-    Engine* e = &h->e;
-    e->qf_raw = q;
+// Buffers of the gradient schedule: lap and the frozen potential for friction
+// or the Weizsaecker term, the gradient sums for the latter.
+static int gradient_buffers(Engine* e) {
     e->lap_valid = false;
-    if (q != 0.0) {
+    cudaStreamSynchronize(e->st);
+    if (e->grad_terms()) {
         if (!e->lap) GPE_CK(cudaMalloc(&e->lap, e->csize() * e->n));
         if (!e->Vqf) GPE_CK(cudaMalloc(&e->Vqf, e->rsize() * e->n));
     } else {
-        cudaStreamSynchronize(e->st);
         cudaFree(e->lap); cudaFree(e->Vqf);
         e->lap = nullptr; e->Vqf = nullptr;
     }
+    if (e->wz != 0.0) {
+        if (!e->wg) GPE_CK(cudaMalloc(&e->wg, e->rsize() * e->n));
+        if (!e->ws) GPE_CK(cudaMalloc(&e->ws, e->rsize() * e->n));
+    } else {
+        cudaFree(e->wg); cudaFree(e->ws);
+        e->wg = nullptr; e->ws = nullptr;
+    }
     return gpe::upload(e);
+}
+
+int gpe_gb_set_quantum_friction_coeff(gpe_gb_engine* h, double q) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    h->e.qf_raw = q;
+    return gradient_buffers(&h->e);
+}
+
+int gpe_gb_set_weizsacker(gpe_gb_engine* h, double lambda) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    Engine* e = &h->e;
+    // FP32 x pencils of 512 points hold 512-thread CTAs whose staged operands with
+    // the gradient sums exceed a CTA's shared memory
+    if (lambda != 0.0 && e->prec == GPE_PRECISION_FP32 && e->n3[0] > 256) return GPE_ERR_LATTICE;
+    e->wz = lambda;
+    return gradient_buffers(e);
 }
 
 static int stage_alloc(Engine* e) {
@@ -1705,7 +1748,7 @@ int gpe_gb_control_create(gpe_gb_control** out, gpe_gb_engine* h, int nbasis, co
     *out = nullptr;
     Engine* e = &h->e;
     if (e->prec != GPE_PRECISION_FP64 || e->beta != 0.0 || e->alpha == 0.0 || e->inter != gpe::INTER_BEC ||
-        e->qf_raw != 0.0)
+        e->grad_terms())
         return GPE_ERR_ARGUMENT;
     if (nbasis <= 0 || nbasis > gpe::kCtlMaxBasis || nslices <= 0 || steps_per_slice <= 0 || checkpoint_every <= 0 ||
         nsteps <= 0 || nsteps % checkpoint_every != 0)

@@ -37,6 +37,7 @@ cudaError_t launch_one(const PassArgs<R>& a, size_t pencils, cudaStream_t st) {
     }
     const unsigned grid = (unsigned)((pencils + Geo::W - 1) / Geo::W);
     const size_t smem = Geo::SMEM_BASE + slot_bytes<R>(staged_ops(a.mid, a.post, a.flags), Geo::E * NT);
+    if (smem > Geo::SMEM_MAX) return cudaErrorInvalidConfiguration;  // more staged operands than a CTA holds
     PassArgs<R> b = a;
     b.npencils = (uint32_t)pencils;
     pass_kernel<R, N, AX, NT, CLS><<<grid, NT, smem, st>>>(b);

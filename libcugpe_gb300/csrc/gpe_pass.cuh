@@ -60,6 +60,7 @@ enum : uint32_t {  // flags
     F_FIN_RED = 1u << 11,   // last CTA: store the NRED sums in dyn->red[red_slot..]
     F_VEXTRA = 1u << 12,    // time-sliced additive potential table
     F_LAP_OUT = 1u << 13,   // after the store: lap = D_a(result) (Laplacian of the new psi)
+    F_WZ = 1u << 14,        // Weizsaecker gradient sums of this axis (wg, ws) from D1_a psi
 };
 
 // Scalars that change while a step runs; they live in device memory so one
@@ -89,7 +90,10 @@ struct PassArgs {
     C2<R>* lap;          // Laplacian accumulator (QF)
     void* aux;           // corrector factor: C2<R> (F_AUX_CPLX) or R
     R* V;                // predictor potential
-    R* Vqf;              // quantum-friction potential
+    R* Vqf;              // frozen gradient potential: quantum friction (+ Weizsaecker)
+    R* wg;               // Weizsaecker: sum over axes done so far of (d_a rho)^2
+    R* ws;               // Weizsaecker: sum over axes done so far of |D1_a psi|^2
+    const R* ld1;        // k_a / N_a of this axis (first derivative)
     const R* vx; const R* vy; const R* vz;   // trap tables
     const R* vextra;     // [slices][n] additive potential (F_VEXTRA)
     int vsteps, vslices;
@@ -231,6 +235,8 @@ enum : uint32_t {
     OP_V = 1u << 4,     // R  V              (corrector)
     OP_AUXR = 1u << 5,  // R  V'             (Vstep3, FP32)
     OP_VQF = 1u << 6,   // R  V_qf           (corrector with friction)
+    OP_WG = 1u << 7,    // R  wg             (Weizsaecker sums, slot C)
+    OP_WS = 1u << 8,    // R  ws             (Weizsaecker sums, slot D)
 };
 
 __host__ __device__ inline uint32_t staged_ops(int mid, int post, uint32_t flags) {
@@ -238,6 +244,10 @@ __host__ __device__ inline uint32_t staged_ops(int mid, int post, uint32_t flags
     if (mid == MID_LAP_ACC) m |= OP_LAP;
     if (mid == MID_QF_VSTEP1) m |= OP_LAP | OP_COPY;
     if (mid == MID_CURRENT) m |= OP_COPY;
+    if (flags & F_WZ) {
+        m |= OP_COPY;
+        if (mid == MID_LAP_ACC || mid == MID_QF_VSTEP1) m |= OP_WG | OP_WS;
+    }
     if (post == POST_VSTEP2 || post == POST_PART12) m |= OP_PSI | OP_V;
     if (post == POST_PART12 && (flags & F_QF)) m |= OP_VQF;
     if (post == POST_PART1) m |= OP_V;
@@ -252,8 +262,8 @@ __host__ __device__ inline size_t slot_bytes(uint32_t m, int per_cta) {
     size_t b = 0;
     if (m & (OP_PSI | OP_LAP | OP_AUXC)) b += (size_t)per_cta * sizeof(C2<R>);
     if (m & OP_COPY) b += (size_t)per_cta * sizeof(C2<R>);
-    if (m & (OP_V | OP_AUXR)) b += (size_t)per_cta * sizeof(R);
-    if (m & OP_VQF) b += (size_t)per_cta * sizeof(R);
+    if (m & (OP_V | OP_AUXR | OP_WG)) b += (size_t)per_cta * sizeof(R);
+    if (m & (OP_VQF | OP_WS)) b += (size_t)per_cta * sizeof(R);
     return b;
 }
 
@@ -298,11 +308,14 @@ struct PassGeom {
     static constexpr size_t TAB_BYTES = (((size_t)(TW + N) * sizeof(C2<R>) + N * sizeof(R)) + 15) & ~(size_t)15;
     static constexpr size_t EXCH_BYTES = (size_t)W * ROW * sizeof(C2<R>);
     static constexpr size_t SMEM_BASE = TAB_BYTES + EXCH_BYTES;
-    // the largest staged-operand set is two complex values per point (psi + V + V_qf, or lap + copy)
-    static constexpr size_t SMEM_MAX = SMEM_BASE + 2 * (size_t)E * NT * sizeof(C2<R>);
+    // the largest staged-operand set: lap + copy + the two Weizsaecker sums (two complex and two
+    // real values per point); a launch that would need more than a CTA can hold is refused
+    static constexpr size_t SMEM_FULL = SMEM_BASE + 2 * (size_t)E * NT * (sizeof(C2<R>) + sizeof(R));
+    static constexpr size_t SMEM_MAX = SMEM_FULL < 232448 ? SMEM_FULL : 232448;
     static constexpr int MINB = ((sizeof(R) == 4 ? 512 : 256) / NT) > 0 ? (sizeof(R) == 4 ? 512 : 256) / NT : 1;
     static_assert(NT % G == 0 && NT % 32 == 0, "threads per CTA must hold whole groups");
-    static_assert(SMEM_MAX <= 232448, "shared memory of a pass exceeds the per-CTA limit");
+    static_assert(SMEM_BASE + 2 * (size_t)E * NT * sizeof(C2<R>) <= 232448,
+                  "shared memory of a pass without the Weizsaecker sums exceeds the per-CTA limit");
 };
 
 // Kernel classes: each instantiation compiles only the code its passes use,
@@ -403,19 +416,20 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
         slotB = reinterpret_cast<C2<R>*>(sop);
         if (ops & OP_COPY) sop += (size_t)E * NT * sizeof(C2<R>);
         slotC = reinterpret_cast<R*>(sop);
-        if (ops & (OP_V | OP_AUXR)) sop += (size_t)E * NT * sizeof(R);
+        if (ops & (OP_V | OP_AUXR | OP_WG)) sop += (size_t)E * NT * sizeof(R);
         slotD = reinterpret_cast<R*>(sop);
         if (ops && valid) {
             const void* srcA = (ops & OP_PSI) ? (const void*)a.psi : (ops & OP_LAP) ? (const void*)a.lap : a.aux;
-            const void* srcC = (ops & OP_V) ? (const void*)a.V : a.aux;
+            const void* srcC = (ops & OP_V) ? (const void*)a.V : (ops & OP_WG) ? (const void*)a.wg : a.aux;
+            const R* srcD = (ops & OP_VQF) ? a.Vqf : a.ws;
 #pragma unroll
             for (int q = 0; q < E; q++) {
                 const uint32_t idx = at(q);
                 if (ops & (OP_PSI | OP_LAP | OP_AUXC))
                     cp_async(slotA + q * NT + tid, reinterpret_cast<const C2<R>*>(srcA) + idx, sizeof(C2<R>));
-                if (ops & (OP_V | OP_AUXR))
+                if (ops & (OP_V | OP_AUXR | OP_WG))
                     cp_async(slotC + q * NT + tid, reinterpret_cast<const R*>(srcC) + idx, sizeof(R));
-                if (ops & OP_VQF) cp_async(slotD + q * NT + tid, a.Vqf + idx, sizeof(R));
+                if (ops & (OP_VQF | OP_WS)) cp_async(slotD + q * NT + tid, srcD + idx, sizeof(R));
             }
         }
         cp_async_commit();
@@ -444,6 +458,43 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
 #pragma unroll
         for (int q = 0; q < E; q++) x[q] = own(q);
     };
+    // Weizsaecker gradient sums along this axis, from x = psi (a copy in slot B):
+    // D1 = IFFT(i k_a FFT psi)/N_a, d_a rho = 2 Gamma Re(conj(psi) D1), and |D1|^2.
+    // mode 0 stores them, 1 adds them to the sums of the earlier axes (rescaled by
+    // the pending norm factor, as they were taken from the unscaled psi), 2 adds
+    // them into slots C/D for the MID op.  x is psi again afterwards.
+    auto wz_grad = [&](int mode) {
+        fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
+#pragma unroll
+        for (int q = 0; q < E; q++) {
+            const R k = __ldg(a.ld1 + t + T * q);
+            x[q] = mk<R>(-k * x[q].y, k * x[q].x);
+        }
+        fft<R, N, true, SSTR, G>(x, sb, t, stw, bar);
+        cp_async_wait_all();
+        if (valid) {
+            const R f2 = scale_in ? s_prev * s_prev : (R)1;
+#pragma unroll
+            for (int q = 0; q < E; q++) {
+                const C2<R> p = slotB[q * NT + tid];
+                const R d = (R)2 * a.ph.gamma * (p.x * x[q].x + p.y * x[q].y);
+                const R g = d * d, s = x[q].x * x[q].x + x[q].y * x[q].y;
+                if (mode == 0) {
+                    a.wg[at(q)] = g;
+                    a.ws[at(q)] = s;
+                } else if (mode == 1) {
+                    a.wg[at(q)] = slotC[q * NT + tid] * (f2 * f2) + g;
+                    a.ws[at(q)] = slotD[q * NT + tid] * f2 + s;
+                } else {
+                    slotC[q * NT + tid] += g;
+                    slotD[q * NT + tid] += s;
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < E; q++) x[q] = slotB[q * NT + tid];
+    };
+    (void)wz_grad;
 
     // ---------------------------------------------------------------- PRE
     if constexpr (CLS == C_EPI || CLS == C_EN) {
@@ -502,6 +553,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
 #pragma unroll
             for (int q = 0; q < E; q++) slotB[q * NT + tid] = x[q];
         }
+        if (a.flags & F_WZ) wz_grad(a.mid == MID_LAP_STORE ? 0 : a.mid == MID_LAP_ACC ? 1 : 2);
         fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
 #pragma unroll
         for (int q = 0; q < E; q++) x[q] = cscale(x[q], slt[t + T * q]);
@@ -528,8 +580,15 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                     const C2<R> L = cadd(slotA[q * NT + tid], own(q));
                     const C2<R> p = slotB[q * NT + tid];
                     const R rho = density(a.ph, p);
-                    // Im(conj(psi) L) / (rho + eps)   (dev/gpe_engine.cu:916)
-                    const R vqf = (p.x * L.y + (-p.y) * L.x) / (rho + a.ph.qf_eps);
+                    // (qf/Gamma) Im(conj(psi) L) / (rho + eps), L = -lap psi   (dev/gpe_engine.cu:893-918)
+                    R vqf = (a.ph.qf_g * (p.x * L.y + (-p.y) * L.x)) / (rho + a.ph.qf_eps);
+                    if (a.flags & F_WZ) {
+                        // (lambda/8) [ |grad rho|^2/rho^2 - 2 lap(rho)/rho ],
+                        // lap rho = 2 Gamma (Re(conj(psi) lap psi) + sum_a |D1_a psi|^2)
+                        const R inv = (R)1 / (rho + a.ph.qf_eps);
+                        const R lrho = (R)2 * a.ph.gamma * (slotD[q * NT + tid] - (p.x * L.x + p.y * L.y));
+                        vqf += a.ph.wz8 * (slotC[q * NT + tid] * inv * inv - (R)2 * lrho * inv);
+                    }
                     a.Vqf[idx] = vqf;
                     const R V = (vext_at(a, idx, ix, iy, iz, it) + dEDFdn(a.ph, rho)) + vqf;
                     a.V[idx] = V;
@@ -613,6 +672,11 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     }
     if constexpr (CLS == C_EPI) {
         if (a.flags & F_LAP_OUT) {
+            if (a.flags & F_WZ) {
+#pragma unroll
+                for (int q = 0; q < E; q++) slotB[q * NT + tid] = x[q];
+                wz_grad(0);
+            }
             fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
 #pragma unroll
             for (int q = 0; q < E; q++) x[q] = cscale(x[q], slt[t + T * q]);

@@ -33,6 +33,8 @@ struct Phys {
     R c_bec;          // (4 pi) a, contact BEC mean field
     R a_scat;         // scattering length (user param A_SCAT)
     R qf_eps;         // 1e-12 (dev/gpe_engine.cuh:53)
+    R qf_g;           // quantum friction coefficient / Gamma
+    R wz8;            // Weizsaecker weight / 8
 };
 
 __device__ __forceinline__ double gexp(double x) { return exp(x); }

@@ -71,6 +71,8 @@ def lib():
         L.oracle_energy.argtypes = [vp, dp, dp, dp, dp]
         L.oracle_energy.restype = i
         L.oracle_get_currents.argtypes = [vp, dp, dp, dp, dp]
+        L.oracle_set_wz.argtypes = [vp, d]
+        L.oracle_wz_potential.argtypes = [vp, dp]
         L.oracle_get_currents.restype = i
         L.oracle_fft3d.argtypes = [i, i, i, dp, i, i]
         L.oracle_set_vortex.argtypes = [vp, d, d, i]
@@ -141,6 +143,15 @@ class Oracle:
         t = ctypes.c_double()
         lib().oracle_get_density(self._h, ctypes.byref(t), _dp(out))
         return t.value, out
+
+    def set_weizsacker(self, lam):
+        lib().oracle_set_wz(self._h, float(lam))
+
+    def wz_potential(self):
+        """V_W = (lambda/8)(|grad rho|^2/rho^2 - 2 lap rho/rho) of the current psi."""
+        out = np.empty(self.shape, dtype=np.float64)
+        lib().oracle_wz_potential(self._h, _dp(out))
+        return out
 
     def get_currents(self):
         """(t, jx, jy, jz) as gpe_get_currents (dev/gpe_engine.cu:1856-1904)."""

@@ -69,6 +69,10 @@ typedef struct {
     double vx0, vy0;
     int vq;
     double *phase;
+    /* Weizsaecker term (not in the reference): weight and scratch */
+    double wz;
+    cd *wz1;
+    double *wzG, *wzS;
 } gpe_oracle;
 
 /* ---------------------------------------------------------------- helpers */
@@ -281,6 +285,7 @@ void oracle_destroy(void *h) {
     free(o->kx); free(o->ky); free(o->kz); free(o->ex); free(o->ey); free(o->ez);
     for (int a = 0; a < 3; a++) free(o->tw[a]);
     free(o->psi); free(o->psi2); free(o->wrkC); free(o->wrk3C); free(o->V); free(o->Vqf); free(o->rho);
+    free(o->wz1); free(o->wzG); free(o->wzS);
     free(o->phase);
     free(o);
 }
@@ -315,6 +320,16 @@ void oracle_set_qf(void *h, double q) {
     /* dev/gpe_engine.cu:435-460 */
     gpe_oracle *o = (gpe_oracle *)h;
     o->qfcoeff = (q != 0.0) ? q / (o->gamma * (double)o->n) : 0.0;
+}
+
+void oracle_set_wz(void *h, double lambda) {
+    gpe_oracle *o = (gpe_oracle *)h;
+    o->wz = lambda;
+    if (lambda != 0.0 && !o->wz1) {
+        o->wz1 = calloc(o->n, sizeof(cd));
+        o->wzG = calloc(o->n, sizeof(double));
+        o->wzS = calloc(o->n, sizeof(double));
+    }
 }
 
 void oracle_set_vextra(void *h, const double *v, int nslices, int steps_per_slice) {
@@ -400,6 +415,71 @@ static void qf_potential(gpe_oracle *o, const cd *psi) {
     }
 }
 
+/* Weizsaecker gradient term, added to Vqf (not in the reference; the hook
+ * gpe_gradient_corrections of dev/gpe_user_defined.h:158 is never called):
+ * E_W = (lambda/8) sum |grad rho|^2 / rho, so
+ * V_W = (lambda/8) (|grad rho|^2 / rho^2 - 2 lap(rho) / rho), rho = Gamma |psi|^2,
+ * grad rho = 2 Gamma Re(conj(psi) grad psi),
+ * lap rho = 2 Gamma (Re(conj(psi) lap psi) + |grad psi|^2),
+ * derivatives of psi spectral on the reference k grid (dev/gpe_engine.cu:147-154),
+ * rho regularised by ORC_QF_EPSILON as in the friction potential. */
+static void wz_potential(gpe_oracle *o, const cd *psi) {
+    const int ny = o->ny, nz = o->nz;
+    const long n = (long)o->n;
+    const double inv_n = 1.0 / (double)o->n, g2 = 2.0 * o->gamma;
+    memcpy(o->wrk3C, psi, sizeof(cd) * o->n);
+    fft3d(o, o->wrk3C, -1);
+    memset(o->wzG, 0, sizeof(double) * o->n);
+    memset(o->wzS, 0, sizeof(double) * o->n);
+    const double *ks[3] = {o->kx, o->ky, o->kz};
+    for (int a = 0; a < 3; a++) {
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+        for (long i = 0; i < n; i++) {
+            DECODE((size_t)i);
+            const double k = ks[a][(a == 0) ? ix : (a == 1) ? iy : iz] * inv_n;
+            cd z; z.x = -k * o->wrk3C[i].y; z.y = k * o->wrk3C[i].x;  /* i k psi_hat / n */
+            o->wz1[i] = z;
+        }
+        fft3d(o, o->wz1, +1);
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+        for (long i = 0; i < n; i++) {
+            const cd p = psi[i], d1 = o->wz1[i];
+            const double d = g2 * (p.x * d1.x + p.y * d1.y);
+            o->wzG[i] += d * d;
+            o->wzS[i] += d1.x * d1.x + d1.y * d1.y;
+        }
+    }
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+    for (long i = 0; i < n; i++) {
+        DECODE((size_t)i);
+        const double k2 = o->kx[ix] * o->kx[ix] + o->ky[iy] * o->ky[iy] + o->kz[iz] * o->kz[iz];
+        o->wz1[i] = cscale(o->wrk3C[i], -k2 * inv_n);
+    }
+    fft3d(o, o->wz1, +1);
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+    for (long i = 0; i < n; i++) {
+        const cd p = psi[i], l = o->wz1[i];
+        const double inv = 1.0 / (density(o, p) + ORC_QF_EPSILON);
+        const double lrho = g2 * ((p.x * l.x + p.y * l.y) + o->wzS[i]);
+        o->Vqf[i] += (o->wz / 8.0) * (o->wzG[i] * inv * inv - 2.0 * lrho * inv);
+    }
+}
+
+/* potential frozen over a step: friction (dev/gpe_engine.cu:893-933) and the Weizsaecker term */
+static void frozen_potential(gpe_oracle *o, const cd *psi) {
+    if (o->qfcoeff != 0.0) qf_potential(o, psi);
+    else memset(o->Vqf, 0, sizeof(double) * o->n);
+    if (o->wz != 0.0) wz_potential(o, psi);
+}
+
+/* V_W alone for the current psi (tests) */
+void oracle_wz_potential(void *h, double *out) {
+    gpe_oracle *o = (gpe_oracle *)h;
+    memset(o->Vqf, 0, sizeof(double) * o->n);
+    if (o->wz != 0.0) wz_potential(o, o->psi);
+    memcpy(out, o->Vqf, sizeof(double) * o->n);
+}
+
 /* enforcing ops: 1 vortex imprint (dev/gpe_engine.cu:485-511), 2 imprint
  * where |psi| > 1e-15 (:520-548), 3 psi = |psi| exp(i phase) (:584-591) */
 static void enforce(gpe_oracle *o, int mode) {
@@ -459,12 +539,12 @@ int oracle_evolve_enforced(void *h, int nt, double *mu, int kind) {
 static int evolve_impl(gpe_oracle *o, int nt, double *mu, int mode, int mid_repeat) {
     const int ny = o->ny, nz = o->nz;
     const long n = (long)o->n;
-    const int qf = o->qfcoeff != 0.0;
+    const int qf = o->qfcoeff != 0.0 || o->wz != 0.0;
     for (int step = 0; step < nt; step++) {
         const unsigned it = o->it;
         if (mode) enforce(o, mode);
         /* Vstep1 / Vstep1_qf: dev/gpe_engine.cu:719-768, 1038-1047 */
-        if (qf) qf_potential(o, o->psi);
+        if (qf) frozen_potential(o, o->psi);
 #pragma omp parallel for num_threads(o->nthreads) schedule(static)
         for (long i = 0; i < n; i++) {
             DECODE((size_t)i);
@@ -500,7 +580,7 @@ static int evolve_impl(gpe_oracle *o, int nt, double *mu, int mode, int mid_repe
                 normalize(o, o->psi2);
                 if (mode && mid_repeat) enforce(o, mode); /* :1161, :1253, :1436 */
             }
-            if (qf) qf_potential(o, o->psi);
+            if (qf) frozen_potential(o, o->psi);
             /* part2 / part2_qf: dev/gpe_engine.cu:813-864 */
 #pragma omp parallel for num_threads(o->nthreads) schedule(static)
             for (long i = 0; i < n; i++) {

@@ -221,3 +221,65 @@ def test_currents_match_oracle(cuda_device, gpe_lib, shape):
     got = e32.get_currents()
     for a in range(1, 4):
         assert rel(got[a], ref[a]) <= 5e-5, (a, rel(got[a], ref[a]))
+
+
+WZ = {"ufg_rte_qf": 0.25, "ufg_ite_qf": 0.25, "ufg_rte": 0.25, "bec_ite": 0.5}
+
+
+def make_wz_pair(shape, case, precision=g.FP64):
+    e, o, psi = make_pair(shape, case, precision=precision)
+    e.set_weizsacker(WZ[case])
+    o.set_weizsacker(WZ[case])
+    return e, o, psi
+
+
+@pytest.mark.parametrize("case", list(WZ))
+@pytest.mark.parametrize("shape", SHAPES[:3])
+def test_weizsacker_fp64_per_step_parity(cuda_device, gpe_lib, case, shape):
+    """Weizsaecker term (new form, oracle-pinned): <= 1e-12 per step against the oracle."""
+    e, o, _ = make_wz_pair(shape, case)
+    beta = CASES[case][2]
+    for step in range(3):
+        mu_e = e.evolve_qf(1)
+        mu_o = o.evolve_qf(1)
+        _, po = o.get_psi()
+        assert rel(e.get_psi()[1], po) <= TOL_FP64_STEP, (step, rel(e.get_psi()[1], po))
+        if beta != 0.0:
+            assert abs(mu_e - mu_o) <= 1e-10 * max(1.0, abs(mu_o))
+        e.set_psi(0.0, po)
+        o.set_psi(0.0, po)
+
+
+@pytest.mark.parametrize("case", ["ufg_rte_qf", "ufg_ite_qf", "ufg_rte"])
+def test_weizsacker_multi_step_fp64_fp32(cuda_device, gpe_lib, case):
+    """30 steps through the replayed step (sums of the z axis carried from the previous step's
+    last pass); the FP32 form within 2e-5 per step; the term changes the evolution."""
+    shape = (32, 16, 16)
+    e, o, psi = make_wz_pair(shape, case)
+    for _ in range(3):
+        e.evolve_qf(10)
+        o.evolve_qf(10)
+    po = o.get_psi()[1]
+    assert rel(e.get_psi()[1], po) <= 3e-11
+    plain, _, _ = make_pair(shape, case)
+    plain.evolve_qf(30)
+    assert rel(plain.get_psi()[1], po) > 1e-6
+    e32, o32, _ = make_wz_pair(shape, case, precision=g.FP32)
+    e32.evolve_qf(1)
+    o32.evolve_qf(1)
+    assert rel(e32.get_psi()[1], o32.get_psi()[1]) <= TOL_FP32_STEP
+    e32.evolve_qf(20)
+    o32.evolve_qf(20)
+    assert rel(e32.get_psi()[1], o32.get_psi()[1]) <= 20 * TOL_FP32_STEP
+
+
+def test_weizsacker_off_restores_plain_step(cuda_device, gpe_lib):
+    shape = (16, 16, 16)
+    e, o, psi = make_pair(shape, "ufg_rte_qf")
+    e.set_weizsacker(0.25)
+    e.evolve_qf(2)
+    e.set_weizsacker(0.0)
+    e.set_psi(0.0, psi)
+    e.evolve_qf(3)
+    o.evolve_qf(3)
+    assert rel(e.get_psi()[1], o.get_psi()[1]) <= 3e-12

@@ -191,3 +191,39 @@ def test_oracle_currents_plane_wave_and_numpy():
         kk = (2 * np.pi * np.fft.fftfreq(shape[a])).reshape([-1 if b == a else 1 for b in range(3)])
         ref = np.real(np.conj(psi) * np.fft.ifftn(kk / gamma * f))
         assert rel(j, ref) < 1e-13, a
+
+
+def test_oracle_weizsacker_potential_gaussian_and_numpy():
+    """V_W = (lambda/8)(|grad rho|^2/rho^2 - 2 lap rho/rho): for rho ~ exp(-sum x_a^2/(2 s_a^2)) it is
+    (lambda/8)(2 sum 1/s_a^2 - sum x_a^2/s_a^4); a random state matches a numpy restatement."""
+    shape, s, lam, gamma = (64, 32, 32), (3.0, 2.0, 2.0), 0.25, 2.0
+    X, Y, Z = [np.arange(n, dtype=float)[tuple(slice(None) if b == a else None for b in range(3))] - n // 2
+               for a, n in enumerate(shape)]
+    psi = np.exp(-X ** 2 / (4 * s[0] ** 2) - Y ** 2 / (4 * s[1] ** 2) - Z ** 2 / (4 * s[2] ** 2)) * np.ones(shape)
+    o = oracle.Oracle(shape, 0, 1.0, 0.0, 0.05, 1000.0, threads=4)
+    o.set_weizsacker(lam)
+    o.set_psi(0.0, psi.astype(np.complex128))
+    vw = o.wz_potential()
+    ref = lam / 8 * (2 * sum(1 / x ** 2 for x in s) - X ** 2 / s[0] ** 4 - Y ** 2 / s[1] ** 4 - Z ** 2 / s[2] ** 4)
+    core = (X / s[0]) ** 2 + (Y / s[1]) ** 2 + (Z / s[2]) ** 2 < 4.0
+    assert np.max(np.abs(vw - ref)[core]) < 1e-9
+    # random state: the same formula with numpy's FFT
+    shape = (16, 8, 32)
+    psi = configs.random_state(shape, seed=13, npart=1000.0, gamma=gamma)
+    o = oracle.Oracle(shape, 0, 1.0, 0.0, 0.05, 1000.0, threads=2)
+    o.set_weizsacker(lam)
+    o.set_psi(0.0, psi)
+    vw = o.wz_potential()
+    f = np.fft.fftn(psi)
+    ks = [(2 * np.pi * np.fft.fftfreq(n)).reshape([-1 if b == a else 1 for b in range(3)]) for a, n in enumerate(shape)]
+    rho = gamma * np.abs(psi) ** 2
+    grad2, sq = 0.0, 0.0
+    for k in ks:
+        d1 = np.fft.ifftn(1j * k * f)
+        grad2 = grad2 + (2 * gamma * np.real(np.conj(psi) * d1)) ** 2
+        sq = sq + np.abs(d1) ** 2
+    lap = np.fft.ifftn(-(ks[0] ** 2 + ks[1] ** 2 + ks[2] ** 2) * f)
+    lrho = 2 * gamma * (np.real(np.conj(psi) * lap) + sq)
+    inv = 1.0 / (rho + 1e-12)
+    ref = lam / 8 * (grad2 * inv ** 2 - 2 * lrho * inv)
+    assert rel(vw, ref) < 1e-12
