@@ -599,6 +599,25 @@ def main():
         extras["fp32_vs_fp64"] = {"steps": nchk, "dE_over_E": abs(Ea - Eb) / abs(Eb),
                                   "density_rel_l2": float(np.linalg.norm(da - db) / np.linalg.norm(db))}
         a.close(); b.close(); e64.close()
+        # the workload with its Weizsaecker gradient term of weight 0.25 (not in the reference:
+        # pinned by the oracle only); FP32 speed and FP32-vs-FP64 error after the same steps
+        aw = make_engine(w, psi, g.FP32)
+        aw.set_weizsacker(0.25)
+        tw, _ = time_blocks(aw, args.block, max(2, args.steps // 2), 1, flush, torch)
+        aw.set_psi(0.0, psi)
+        bw = make_engine(w, psi, g.FP64)
+        bw.set_weizsacker(0.25)
+        aw.evolve_qf(nchk)
+        bw.evolve_qf(nchk)
+        ea, eb = aw.energy(), bw.energy()
+        Ea, Eb = sum(ea[1:]), sum(eb[1:])
+        _, da = aw.get_density()
+        _, db = bw.get_density()
+        extras["weizsacker_0.25"] = {
+            "value": max(2, args.steps // 2) * args.block / tw, "unit": "steps/s", "dtype": "f32",
+            "fp32_vs_fp64": {"steps": nchk, "dE_over_E_without_EW": abs(Ea - Eb) / abs(Eb),
+                             "density_rel_l2": float(np.linalg.norm(da - db) / np.linalg.norm(db))}}
+        aw.close(); bw.close()
         ref = reference_gpu(w, psi)
         if ref:
             extras["reference_gpu"] = ref
