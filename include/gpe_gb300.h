@@ -60,11 +60,18 @@ int gpe_gb_set_quantum_friction_coeff(gpe_gb_engine* e, double qfcoeff);
  * reference declares gpe_gradient_corrections, dev/gpe_user_defined.h:158,
  * but never calls it).  Adds E_W = (lambda/8) sum |grad rho|^2 / rho to the
  * functional, i.e. V_W = (lambda/8) (|grad rho|^2/rho^2 - 2 lap(rho)/rho)
- * (lattice units, hbar = m = 1, rho = Gamma |psi|^2, rho regularised by
- * +1e-12), with spectral derivatives of psi.  Like the friction potential,
- * V_W is evaluated once per step at the step's initial psi and enters both
- * halves of the step.  0 turns it off.  FP32 form: x side <= 256. */
-int gpe_gb_set_weizsacker(gpe_gb_engine* e, double lambda);
+ * (lattice units, hbar = m = 1, rho = Gamma |psi|^2), with spectral
+ * derivatives of psi and rho replaced by rho + eps in both denominators, so
+ * V_W fades out where rho << eps (the far tails, whose derivatives are
+ * round-off); eps <= 0 selects 1e-2 npart / (nx ny nz).  Like the friction
+ * potential, V_W is evaluated once per step at the step's initial psi and
+ * enters both halves of the step.  That explicit treatment of a term that
+ * stiffens like k^2 is stable for dt |lambda| 3 pi^2 <= 0.4, so while the
+ * term is on a step of dt runs as m = ceil(dt |lambda| 3 pi^2 / 0.4) equal
+ * sub-steps (evolve(nt) still advances nt dt; the time-sliced potential's
+ * steps_per_slice still counts steps of dt).  lambda = 0 turns it off.
+ * FP32 form: x side <= 256. */
+int gpe_gb_set_weizsacker(gpe_gb_engine* e, double lambda, double eps);
 /* gpe_set_psi (dev/gpe_engine.cu:694): psi = 2*nx*ny*nz doubles */
 int gpe_gb_set_psi(gpe_gb_engine* e, double t, const double* psi);
 /* gpe_get_psi (dev/gpe_engine.cu:705) */

@@ -79,7 +79,7 @@ def _lib():
             "gpe_gb_set_time": (i, [vp, d]),
             "gpe_gb_set_user_params": (i, [vp, i, dp]),
             "gpe_gb_set_quantum_friction_coeff": (i, [vp, d]),
-            "gpe_gb_set_weizsacker": (i, [vp, d]),
+            "gpe_gb_set_weizsacker": (i, [vp, d, d]),
             "gpe_gb_set_psi": (i, [vp, d, dp]),
             "gpe_gb_get_psi": (i, [vp, dp, dp]),
             "gpe_gb_get_density": (i, [vp, dp, dp]),
@@ -197,9 +197,11 @@ class Engine:
     def set_quantum_friction_coeff(self, q):
         _check(_lib().gpe_gb_set_quantum_friction_coeff(self._h, float(q)), "set_quantum_friction_coeff")
 
-    def set_weizsacker(self, lam):
-        """Weizsaecker gradient term (lambda/8) |grad rho|^2/rho in the functional; 0 turns it off."""
-        _check(_lib().gpe_gb_set_weizsacker(self._h, float(lam)), "set_weizsacker")
+    def set_weizsacker(self, lam, eps=0.0):
+        """Weizsaecker gradient term (lambda/8) |grad rho|^2/(rho + eps) in the functional; lam = 0 turns
+        it off, eps <= 0 selects 1e-2 npart / n.  Steps longer than the term's stability bound
+        (dt |lam| 3 pi^2 <= 0.4) run as equal sub-steps."""
+        _check(_lib().gpe_gb_set_weizsacker(self._h, float(lam), float(eps)), "set_weizsacker")
 
     def set_psi(self, t, psi):
         p = np.ascontiguousarray(psi, dtype=np.complex128).reshape(self.shape)

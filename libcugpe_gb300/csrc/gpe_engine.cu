@@ -202,7 +202,10 @@ struct Engine {
     double gamma = 1.0;
     int prec = GPE_PRECISION_FP64;
     double alpha = 0, beta = 0, dt = 0, npart = 1, t0 = 0, qf_raw = 0;
-    double wz = 0;  // Weizsaecker weight lambda (0: off)
+    double wz = 0;      // Weizsaecker weight lambda (0: off)
+    double wz_eps = 0;  // its density regularisation
+    double dt_step = 0; // the caller's time step; dt = dt_step / sub
+    int sub = 1;        // internal sub-steps per step (the Weizsaecker term's stability bound)
     unsigned it = 0;
     double up[32] = {0};
     cudaStream_t st = nullptr;
@@ -374,6 +377,7 @@ static Phys<R> make_phys(const Engine* e) {
     p.qf_eps = (R)1.0e-12;
     p.qf_g = (R)(e->qf_raw / e->gamma);
     p.wz8 = (R)(e->wz / 8.0);
+    p.wz_eps = (R)e->wz_eps;
     return p;
 }
 
@@ -455,7 +459,7 @@ static PassArgs<R> base_args(const Engine* e) {
     a.vy = (const R*)e->ax[1].vt;
     a.vz = (const R*)e->ax[2].vt;
     a.vextra = (const R*)e->vextra;
-    a.vsteps = e->vsteps;
+    a.vsteps = e->vsteps * e->sub;
     a.vslices = e->vslices;
     a.dyn = e->dyn;
     a.partials = e->partials;
@@ -1287,6 +1291,7 @@ int gpe_gb_create(gpe_gb_engine** out, int nx, int ny, int nz, int interactions,
     e->gamma = (interactions == -1) ? 1.0 : 2.0;  // GPE_FOR defaults, dev/gpe_user_defined.h:104,182,289
     e->prec = precision;
     e->alpha = alpha; e->beta = beta; e->dt = dt; e->npart = npart;
+    e->dt_step = dt;
     const size_t cs = e->csize(), rs = e->rsize();
     int rc = 0;
     cudaError_t ce;
@@ -1380,13 +1385,20 @@ int gpe_gb_set_quantum_friction_coeff(gpe_gb_engine* h, double q) {
     return gradient_buffers(&h->e);
 }
 
-int gpe_gb_set_weizsacker(gpe_gb_engine* h, double lambda) {
+int gpe_gb_set_weizsacker(gpe_gb_engine* h, double lambda, double eps) {
     if (!h) return GPE_ERR_NO_ENGINE;
     Engine* e = &h->e;
     // FP32 x pencils of 512 points hold 512-thread CTAs whose staged operands with
     // the gradient sums exceed a CTA's shared memory
     if (lambda != 0.0 && e->prec == GPE_PRECISION_FP32 && e->n3[0] > 256) return GPE_ERR_LATTICE;
     e->wz = lambda;
+    e->wz_eps = (eps > 0.0) ? eps : 1e-2 * e->npart / (double)e->n;
+    // V_W is frozen over a step, an explicit treatment of a term that stiffens like k^2: the step
+    // is stable for dt * |lambda| * |k|^2_max <= 0.4 (|k|^2_max = 3 pi^2 on the lattice), so a
+    // longer step runs as `sub` equal sub-steps
+    const double x = e->dt_step * fabs(lambda) * 3.0 * M_PI * M_PI;
+    e->sub = (x > 0.4) ? (int)ceil(x / 0.4) : 1;
+    e->dt = e->dt_step / e->sub;
     return gradient_buffers(e);
 }
 
@@ -1517,7 +1529,7 @@ int gpe_gb_normalize_psi(gpe_gb_engine* h) {
 int gpe_gb_evolve_qf(gpe_gb_engine* h, int nt, double* mu) {
     if (!h) return GPE_ERR_NO_ENGINE;
     Engine* e = &h->e;
-    GPE_RC(gpe::evolve(e, nt, mu));
+    GPE_RC(gpe::evolve(e, nt * e->sub, mu));
     return gpe::cuda_rc(cudaStreamSynchronize(e->st));
 }
 
@@ -1650,7 +1662,7 @@ int gpe_gb_evolve_vortex(gpe_gb_engine* h, int nt, double* mu, int method) {
     if (method < 1 || method > 3) return GPE_ERR_ARGUMENT;
     Engine* e = &h->e;
     // methods 1 and 3 differ only in the mid-step repeat, which is not needed (see evolve_enforced)
-    GPE_RC(gpe::evolve_enforced(e, nt, mu, method == 2 ? gpe::ENF_VORTEX2 : gpe::ENF_VORTEX));
+    GPE_RC(gpe::evolve_enforced(e, nt * e->sub, mu, method == 2 ? gpe::ENF_VORTEX2 : gpe::ENF_VORTEX));
     return gpe::cuda_rc(cudaStreamSynchronize(e->st));
 }
 
@@ -1658,7 +1670,7 @@ int gpe_gb_evolve_enforced_phase(gpe_gb_engine* h, int nt, double* mu) {
     if (!h) return GPE_ERR_NO_ENGINE;
     Engine* e = &h->e;
     if (!e->phase_set) return GPE_ERR_ARGUMENT;
-    GPE_RC(gpe::evolve_enforced(e, nt, mu, gpe::ENF_PHASE));
+    GPE_RC(gpe::evolve_enforced(e, nt * e->sub, mu, gpe::ENF_PHASE));
     return gpe::cuda_rc(cudaStreamSynchronize(e->st));
 }
 

@@ -585,7 +585,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                     if (a.flags & F_WZ) {
                         // (lambda/8) [ |grad rho|^2/rho^2 - 2 lap(rho)/rho ],
                         // lap rho = 2 Gamma (Re(conj(psi) lap psi) + sum_a |D1_a psi|^2)
-                        const R inv = (R)1 / (rho + a.ph.qf_eps);
+                        const R inv = (R)1 / (rho + a.ph.wz_eps);
                         const R lrho = (R)2 * a.ph.gamma * (slotD[q * NT + tid] - (p.x * L.x + p.y * L.y));
                         vqf += a.ph.wz8 * (slotC[q * NT + tid] * inv * inv - (R)2 * lrho * inv);
                     }

@@ -35,6 +35,7 @@ struct Phys {
     R qf_eps;         // 1e-12 (dev/gpe_engine.cuh:53)
     R qf_g;           // quantum friction coefficient / Gamma
     R wz8;            // Weizsaecker weight / 8
+    R wz_eps;         // density regularisation of the Weizsaecker potential
 };
 
 __device__ __forceinline__ double gexp(double x) { return exp(x); }

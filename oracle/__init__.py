@@ -71,7 +71,7 @@ def lib():
         L.oracle_energy.argtypes = [vp, dp, dp, dp, dp]
         L.oracle_energy.restype = i
         L.oracle_get_currents.argtypes = [vp, dp, dp, dp, dp]
-        L.oracle_set_wz.argtypes = [vp, d]
+        L.oracle_set_wz.argtypes = [vp, d, d]
         L.oracle_wz_potential.argtypes = [vp, dp]
         L.oracle_get_currents.restype = i
         L.oracle_fft3d.argtypes = [i, i, i, dp, i, i]
@@ -144,8 +144,8 @@ class Oracle:
         lib().oracle_get_density(self._h, ctypes.byref(t), _dp(out))
         return t.value, out
 
-    def set_weizsacker(self, lam):
-        lib().oracle_set_wz(self._h, float(lam))
+    def set_weizsacker(self, lam, eps=0.0):
+        lib().oracle_set_wz(self._h, float(lam), float(eps))
 
     def wz_potential(self):
         """V_W = (lambda/8)(|grad rho|^2/rho^2 - 2 lap rho/rho) of the current psi."""

@@ -70,7 +70,9 @@ typedef struct {
     int vq;
     double *phase;
     /* Weizsaecker term (not in the reference): weight and scratch */
-    double wz;
+    double wz, wz_eps;
+    double dt_step;       /* the caller's time step; dt = dt_step / sub */
+    int sub;              /* sub-steps per step while the Weizsaecker term is on */
     cd *wz1;
     double *wzG, *wzS;
 } gpe_oracle;
@@ -188,7 +190,7 @@ static inline double vext(const gpe_oracle *o, size_t idx, int ix, int iy, int i
     const double _iz = (double)iz - 1.0 * (o->nz / 2);
     double v = 0.5 * _ix * _ix * wx * wx + 0.5 * _iy * _iy * wy * wy + 0.5 * _iz * _iz * wz * wz;
     if (o->vextra) {
-        int s = (int)(it / (unsigned)o->steps_per_slice);
+        int s = (int)(it / ((unsigned)o->steps_per_slice * (unsigned)o->sub));
         if (s >= o->nslices) s = o->nslices - 1;
         v += o->vextra[(size_t)s * o->n + idx];
     }
@@ -266,6 +268,7 @@ void *oracle_create(int nx, int ny, int nz, int inter, double gamma,
     o->n = (size_t)nx * ny * nz;
     o->inter = inter; o->gamma = gamma;
     o->alpha = alpha; o->beta = beta; o->dt = dt; o->npart = npart;
+    o->dt_step = dt; o->sub = 1;
     o->nthreads = 1;
     o->kx = malloc(sizeof(double) * nx); o->ky = malloc(sizeof(double) * ny); o->kz = malloc(sizeof(double) * nz);
     fill_k(o->kx, nx); fill_k(o->ky, ny); fill_k(o->kz, nz);
@@ -322,9 +325,15 @@ void oracle_set_qf(void *h, double q) {
     o->qfcoeff = (q != 0.0) ? q / (o->gamma * (double)o->n) : 0.0;
 }
 
-void oracle_set_wz(void *h, double lambda) {
+void oracle_set_wz(void *h, double lambda, double eps) {
     gpe_oracle *o = (gpe_oracle *)h;
     o->wz = lambda;
+    o->wz_eps = (eps > 0.0) ? eps : 1e-2 * o->npart / (double)o->n;
+    /* the frozen V_W is stable for dt |lambda| 3 pi^2 <= 0.4: longer steps run as sub-steps */
+    const double x = o->dt_step * fabs(lambda) * 3.0 * M_PI * M_PI;
+    o->sub = (x > 0.4) ? (int)ceil(x / 0.4) : 1;
+    o->dt = o->dt_step / o->sub;
+    tables(o);
     if (lambda != 0.0 && !o->wz1) {
         o->wz1 = calloc(o->n, sizeof(cd));
         o->wzG = calloc(o->n, sizeof(double));
@@ -422,7 +431,7 @@ static void qf_potential(gpe_oracle *o, const cd *psi) {
  * grad rho = 2 Gamma Re(conj(psi) grad psi),
  * lap rho = 2 Gamma (Re(conj(psi) lap psi) + |grad psi|^2),
  * derivatives of psi spectral on the reference k grid (dev/gpe_engine.cu:147-154),
- * rho regularised by ORC_QF_EPSILON as in the friction potential. */
+ * rho replaced by rho + wz_eps in both denominators. */
 static void wz_potential(gpe_oracle *o, const cd *psi) {
     const int ny = o->ny, nz = o->nz;
     const long n = (long)o->n;
@@ -459,7 +468,7 @@ static void wz_potential(gpe_oracle *o, const cd *psi) {
 #pragma omp parallel for num_threads(o->nthreads) schedule(static)
     for (long i = 0; i < n; i++) {
         const cd p = psi[i], l = o->wz1[i];
-        const double inv = 1.0 / (density(o, p) + ORC_QF_EPSILON);
+        const double inv = 1.0 / (density(o, p) + o->wz_eps);
         const double lrho = g2 * ((p.x * l.x + p.y * l.y) + o->wzS[i]);
         o->Vqf[i] += (o->wz / 8.0) * (o->wzG[i] * inv * inv - 2.0 * lrho * inv);
     }
@@ -527,13 +536,17 @@ void oracle_set_phase(void *h, const double *ph) {
 
 static int evolve_impl(gpe_oracle *o, int nt, double *mu, int mode, int mid_repeat);
 
-int oracle_evolve_qf(void *h, int nt, double *mu) { return evolve_impl((gpe_oracle *)h, nt, mu, 0, 0); }
+int oracle_evolve_qf(void *h, int nt, double *mu) {
+    gpe_oracle *o = (gpe_oracle *)h;
+    return evolve_impl(o, nt * o->sub, mu, 0, 0);
+}
 
 /* gpe_evolve_vortex{,2,3} and gpe_evolve_enforced_phase (dev/gpe_engine.cu:1115-1477):
  * kind 1, 2, 3 vortex methods, 4 enforced phase */
 int oracle_evolve_enforced(void *h, int nt, double *mu, int kind) {
     const int mode = (kind == 2) ? 2 : (kind == 4) ? 3 : 1;
-    return evolve_impl((gpe_oracle *)h, nt, mu, mode, kind != 3);
+    gpe_oracle *o = (gpe_oracle *)h;
+    return evolve_impl(o, nt * o->sub, mu, mode, kind != 3);
 }
 
 static int evolve_impl(gpe_oracle *o, int nt, double *mu, int mode, int mid_repeat) {

@@ -283,3 +283,16 @@ def test_weizsacker_off_restores_plain_step(cuda_device, gpe_lib):
     e.evolve_qf(3)
     o.evolve_qf(3)
     assert rel(e.get_psi()[1], o.get_psi()[1]) <= 3e-12
+
+
+def test_weizsacker_substeps_keep_the_step_length(cuda_device, gpe_lib):
+    """A step beyond the stability bound (dt |lambda| 3 pi^2 > 0.4) runs as sub-steps; evolve(nt)
+    still advances nt dt and matches the oracle, which sub-steps the same way."""
+    shape = (16, 16, 16)
+    e, o, _ = make_pair(shape, "ufg_rte_qf", dt=0.125)
+    e.set_weizsacker(0.25)
+    o.set_weizsacker(0.25)
+    e.evolve_qf(4)
+    o.evolve_qf(4)
+    assert e.get_psi()[0] == pytest.approx(0.5)
+    assert rel(e.get_psi()[1], o.get_psi()[1]) <= 1e-11

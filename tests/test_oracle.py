@@ -201,7 +201,7 @@ def test_oracle_weizsacker_potential_gaussian_and_numpy():
                for a, n in enumerate(shape)]
     psi = np.exp(-X ** 2 / (4 * s[0] ** 2) - Y ** 2 / (4 * s[1] ** 2) - Z ** 2 / (4 * s[2] ** 2)) * np.ones(shape)
     o = oracle.Oracle(shape, 0, 1.0, 0.0, 0.05, 1000.0, threads=4)
-    o.set_weizsacker(lam)
+    o.set_weizsacker(lam, 1e-14)
     o.set_psi(0.0, psi.astype(np.complex128))
     vw = o.wz_potential()
     ref = lam / 8 * (2 * sum(1 / x ** 2 for x in s) - X ** 2 / s[0] ** 4 - Y ** 2 / s[1] ** 4 - Z ** 2 / s[2] ** 4)
@@ -211,6 +211,7 @@ def test_oracle_weizsacker_potential_gaussian_and_numpy():
     shape = (16, 8, 32)
     psi = configs.random_state(shape, seed=13, npart=1000.0, gamma=gamma)
     o = oracle.Oracle(shape, 0, 1.0, 0.0, 0.05, 1000.0, threads=2)
+    eps = 1e-2 * 1000.0 / np.prod(shape)  # the default regularisation
     o.set_weizsacker(lam)
     o.set_psi(0.0, psi)
     vw = o.wz_potential()
@@ -224,6 +225,6 @@ def test_oracle_weizsacker_potential_gaussian_and_numpy():
         sq = sq + np.abs(d1) ** 2
     lap = np.fft.ifftn(-(ks[0] ** 2 + ks[1] ** 2 + ks[2] ** 2) * f)
     lrho = 2 * gamma * (np.real(np.conj(psi) * lap) + sq)
-    inv = 1.0 / (rho + 1e-12)
+    inv = 1.0 / (rho + eps)
     ref = lam / 8 * (grad2 * inv ** 2 - 2 * lrho * inv)
     assert rel(vw, ref) < 1e-12
