@@ -91,6 +91,47 @@ def ufg_vortex_rte_qf(n=128, dx=0.2, omega=(1.0, 1.0, 1.5), xi_qf=0.1, dt=5e-3, 
                     xi_qf, steps, psi)
 
 
+def ufg_vortex_lines(n=512, dx=0.1, omega=1.0, xi_qf=0.2, dt=2e-3, steps=5000, npart=5.0e4, lines=8,
+                     radius=4.0, seed=0) -> Workload:
+    """Large cooling run: unitary Fermi gas (dimers) with quantum friction, isotropic trap, Thomas-Fermi
+    profile of the reference functional times `lines` straight vortex lines along z, of charge +1 at
+    seeded positions uniform in the disk of `radius` (oscillator units) of the x-y plane.  npart is not
+    fixed by the problem statement; 5e4 gives a Thomas-Fermi radius of about 8 oscillator lengths."""
+    rng = np.random.default_rng(seed)
+    shape = (n, n, n)
+    w = omega * dx * dx
+    ii = np.arange(n, dtype=np.int64) - n // 2
+    idx = ii.astype(np.float64)
+    X, Y = idx[:, None], idx[None, :]
+    # the trap depends on the integer r^2 only: bisect mu on the histogram of r^2
+    r2 = (ii[:, None, None] ** 2 + ii[None, :, None] ** 2).astype(np.int32) + (ii[None, None, :] ** 2).astype(np.int32)
+    count = np.bincount(r2.ravel())
+    v = 0.5 * w * w * np.arange(count.size, dtype=np.float64)
+
+    def tf_density(mu):
+        return np.maximum(mu - v, 0.0) ** 1.5 / (0.185 ** 1.5 * 3.0 * np.pi ** 2)
+
+    lo, hi = 0.0, float(v.max())
+    for _ in range(80):
+        mid = 0.5 * (lo + hi)
+        if (count * tf_density(mid)).sum() > npart:
+            hi = mid
+        else:
+            lo = mid
+    amp = np.sqrt(tf_density(0.5 * (lo + hi)) / 2.0)[r2]
+    del r2
+    rr = radius / dx * np.sqrt(rng.uniform(0.0, 1.0, lines))
+    th = rng.uniform(0.0, 2.0 * np.pi, lines)
+    phase = np.zeros((n, n))
+    for r, t in zip(rr, th):
+        phase += np.arctan2(Y - r * np.sin(t) + 0.5, X - r * np.cos(t) + 0.5)
+    psi = (amp * np.exp(1j * phase)[:, :, None]).astype(np.complex128)
+    del amp
+    psi = normalise(psi, npart, 2.0)
+    return Workload("ufg_cool_%d" % n, shape, 0, 1.0, 0.0, dt / (dx * dx), npart, [w, w, w, 0.0], xi_qf, steps,
+                    psi)
+
+
 def random_state(shape, seed=0, npart=1.0, gamma=1.0, width=None, phase=True):
     """Seeded smooth complex test state for parity checks."""
     rng = np.random.default_rng(seed)

@@ -311,10 +311,12 @@ struct PassGeom {
     // the largest staged-operand set: lap + copy + the two Weizsaecker sums (two complex and two
     // real values per point); a launch that would need more than a CTA can hold is refused
     static constexpr size_t SMEM_FULL = SMEM_BASE + 2 * (size_t)E * NT * (sizeof(C2<R>) + sizeof(R));
-    static constexpr size_t SMEM_MAX = SMEM_FULL < 232448 ? SMEM_FULL : 232448;
+    // dynamic shared memory cap: the 227 KiB per-CTA opt-in limit less room for the static arrays
+    static constexpr size_t SMEM_CAP = 225 * 1024;
+    static constexpr size_t SMEM_MAX = SMEM_FULL < SMEM_CAP ? SMEM_FULL : SMEM_CAP;
     static constexpr int MINB = ((sizeof(R) == 4 ? 512 : 256) / NT) > 0 ? (sizeof(R) == 4 ? 512 : 256) / NT : 1;
     static_assert(NT % G == 0 && NT % 32 == 0, "threads per CTA must hold whole groups");
-    static_assert(SMEM_BASE + 2 * (size_t)E * NT * sizeof(C2<R>) <= 232448,
+    static_assert(SMEM_BASE + 2 * (size_t)E * NT * sizeof(C2<R>) <= SMEM_CAP,
                   "shared memory of a pass without the Weizsaecker sums exceeds the per-CTA limit");
 };
 
