@@ -217,6 +217,14 @@ int gpe_gb_dftc_write_info(const char* dftc_path, const char* system, const char
 int gpe_gb_dftc_read_info(const char* dftc_path, char* system, char* mode, int len, int* nx, int* ny, int* nz,
                           double* dt, int* nom, double* a_scat, double* aspect_ratio, double* omega_x, double* r0,
                           double* npart, double* total_time);
+/* gpe_evolve_dipolar (dev/gpe_engine.cu:1550-1602): nt Strang steps of the
+ * dipolar BEC (interactions -2; user params OMEGA_X..Z, A_CON, A_DIP), the
+ * contact + dipole-dipole potential recomputed by convolution for each half
+ * step, no friction; ITE normalises each step and returns mu (may be NULL). */
+int gpe_gb_evolve_dipolar(gpe_gb_engine* e, int nt, double* chemical_potential);
+/* gpe_energy_dipolar2 (dev/gpe_engine.cu:1789-1809): E_dip = 1/2 sum rho vdip.
+ * Also serves gpe_energy_dipolar (:1740), the same sum taken in k space. */
+int gpe_gb_energy_dipolar(gpe_gb_engine* e, double* t, double* edip);
 /* Message for a return code. */
 const char* gpe_gb_error_string(int code);
 

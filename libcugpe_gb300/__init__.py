@@ -49,6 +49,7 @@ C_ABI_SYMBOLS = [
     "gpe_gb_batch_kernel_launches", "gpe_gb_chemical_potential", "gpe_gb_control_create", "gpe_gb_control_loss",
     "gpe_gb_control_loss_grad", "gpe_gb_control_destroy", "gpe_gb_snapshots_open", "gpe_gb_snapshots_push",
     "gpe_gb_snapshots_close", "gpe_gb_dftc_write_info", "gpe_gb_dftc_read_info", "gpe_gb_set_weizsacker",
+    "gpe_gb_evolve_dipolar", "gpe_gb_energy_dipolar",
 ]
 
 
@@ -80,6 +81,8 @@ def _lib():
             "gpe_gb_set_user_params": (i, [vp, i, dp]),
             "gpe_gb_set_quantum_friction_coeff": (i, [vp, d]),
             "gpe_gb_set_weizsacker": (i, [vp, d, d]),
+            "gpe_gb_evolve_dipolar": (i, [vp, i, dp]),
+            "gpe_gb_energy_dipolar": (i, [vp, dp, dp]),
             "gpe_gb_set_psi": (i, [vp, d, dp]),
             "gpe_gb_get_psi": (i, [vp, dp, dp]),
             "gpe_gb_get_density": (i, [vp, dp, dp]),
@@ -247,6 +250,18 @@ class Engine:
         mu = ctypes.c_double(0.0)
         _check(_lib().gpe_gb_evolve_qf(self._h, int(nt), ctypes.byref(mu)), "evolve_qf")
         return mu.value
+
+    def evolve_dipolar(self, nt):
+        """gpe_evolve_dipolar: nt steps of the dipolar BEC (interactions -2); mu in ITE."""
+        mu = ctypes.c_double(0.0)
+        _check(_lib().gpe_gb_evolve_dipolar(self._h, int(nt), ctypes.byref(mu)), "evolve_dipolar")
+        return mu.value
+
+    def energy_dipolar(self):
+        """(t, E_dip) with E_dip = 1/2 sum rho vdip."""
+        t, ed = ctypes.c_double(), ctypes.c_double()
+        _check(_lib().gpe_gb_energy_dipolar(self._h, ctypes.byref(t), ctypes.byref(ed)), "energy_dipolar")
+        return t.value, ed.value
 
     def set_vortex(self, x0, y0, q=1):
         _check(_lib().gpe_gb_set_vortex(self._h, float(x0), float(y0), int(q)), "set_vortex")

@@ -99,7 +99,10 @@ int gpe_get_currents(double* t, double* jx, double* jy, double* jz) {
     if (!g_engine) return GPE_ERR_NO_ENGINE;
     return gpe_gb_get_currents(g_engine, t, jx, jy, jz);
 }
-int gpe_evolve_dipolar(int) { return GPE_ERR_NOT_IMPLEMENTED; }
-int gpe_evolve_dipolar(int, double*) { return GPE_ERR_NOT_IMPLEMENTED; }
-int gpe_energy_dipolar(double*, double*) { return GPE_ERR_NOT_IMPLEMENTED; }
-int gpe_energy_dipolar2(double*, double*) { return GPE_ERR_NOT_IMPLEMENTED; }
+int gpe_evolve_dipolar(int nt) { return gpe_gb_evolve_dipolar(g_engine, nt, nullptr); }
+int gpe_evolve_dipolar(int nt, double* mu) { return gpe_gb_evolve_dipolar(g_engine, nt, mu); }
+// The reference sums rho(k) Vpp(k) rho(-k) in k space, indexing -k as n - i, which for the
+// i = 0 planes reads past the transform (dev/gpe_engine.cu:1725); the intended value equals the
+// real-space sum of gpe_energy_dipolar2 (Parseval), which both entry points return.
+int gpe_energy_dipolar(double* t, double* edip) { return gpe_gb_energy_dipolar(g_engine, t, edip); }
+int gpe_energy_dipolar2(double* t, double* edip) { return gpe_gb_energy_dipolar(g_engine, t, edip); }

@@ -192,6 +192,7 @@ struct AxisTables {
     void* vt;     // R[N]      0.5 i^2 w^2, i = index - N/2
     void* lcur;   // R[N]      k / (Gamma N)   (probability currents)
     void* ld1;    // R[N]      k / N           (first derivative, Weizsaecker term)
+    void* kk;     // R[N]      k               (dipolar kernel)
 };
 
 struct Engine {
@@ -311,7 +312,7 @@ static int upload_tables(Engine* e) {
     size_t off = 0;
     std::vector<unsigned char> host;
     size_t total = 0;
-    for (int a = 0; a < 3; a++) total += (size_t)e->n3[a] * (3 * sizeof(C2<R>) + 5 * sizeof(R)) + 256 * 7;
+    for (int a = 0; a < 3; a++) total += (size_t)e->n3[a] * (3 * sizeof(C2<R>) + 6 * sizeof(R)) + 256 * 8;
     host.assign(total, 0);
     if (!e->tabmem) GPE_CK(cudaMalloc(&e->tabmem, total));
     unsigned char* dbase = (unsigned char*)e->tabmem;
@@ -322,7 +323,7 @@ static int upload_tables(Engine* e) {
         kgrid(k, N);
         const size_t okt = take(N * sizeof(C2<R>)), olq = take(N * sizeof(R)), ole = take(N * sizeof(R)),
                      otw = take(2 * N * sizeof(C2<R>)), ovt = take(N * sizeof(R)), ocu = take(N * sizeof(R)),
-                     od1 = take(N * sizeof(R));
+                     od1 = take(N * sizeof(R)), okk = take(N * sizeof(R));
         C2<R>* kt = (C2<R>*)(host.data() + okt);
         R* lq = (R*)(host.data() + olq);
         R* le = (R*)(host.data() + ole);
@@ -330,6 +331,7 @@ static int upload_tables(Engine* e) {
         R* vt = (R*)(host.data() + ovt);
         R* cu = (R*)(host.data() + ocu);
         R* d1 = (R*)(host.data() + od1);
+        R* kq = (R*)(host.data() + okk);
         const double w = e->up[a];
         for (int i = 0; i < N; i++) {
             // exp(c3 k^2 / Gamma^2) (dev/gpe_engine.cu:186-216), with 1/N_a of the unnormalised inverse
@@ -345,11 +347,13 @@ static int upload_tables(Engine* e) {
             vt[i] = (R)(0.5 * ii * ii * w * w);  // dev/gpe_user_defined.h:500-510
             cu[i] = (R)(k[i] / (e->gamma * (double)N));  // dev/gpe_engine.cu:1826 with 1/N_a of the inverse
             d1[i] = (R)(k[i] / (double)N);
+            kq[i] = (R)k[i];
         }
         e->ax[a].ktab = dbase + okt; e->ax[a].lqf = dbase + olq; e->ax[a].lek = dbase + ole;
         stage_twiddles<R>(N, tw);
         e->ax[a].tw = dbase + otw; e->ax[a].vt = dbase + ovt; e->ax[a].lcur = dbase + ocu;
         e->ax[a].ld1 = dbase + od1;
+        e->ax[a].kk = dbase + okk;
     }
     GPE_CK(cudaMemcpyAsync(e->tabmem, host.data(), off, cudaMemcpyHostToDevice, e->st));
     GPE_CK(cudaStreamSynchronize(e->st));
@@ -378,6 +382,8 @@ static Phys<R> make_phys(const Engine* e) {
     p.qf_g = (R)(e->qf_raw / e->gamma);
     p.wz8 = (R)(e->wz / 8.0);
     p.wz_eps = (R)e->wz_eps;
+    p.a_dip = (R)e->up[4];
+    p.nxyz = (R)(double)e->n;
     return p;
 }
 
@@ -455,6 +461,9 @@ static PassArgs<R> base_args(const Engine* e) {
     a.Vqf = (R*)e->Vqf;
     a.wg = (R*)e->wg;
     a.ws = (R*)e->ws;
+    a.kgx = (const R*)e->ax[0].kk;
+    a.kgy = (const R*)e->ax[1].kk;
+    a.kgz = (const R*)e->ax[2].kk;
     a.vx = (const R*)e->ax[0].vt;
     a.vy = (const R*)e->ax[1].vt;
     a.vz = (const R*)e->ax[2].vt;
@@ -663,6 +672,64 @@ static int evolve(Engine* e, int nt, double* mu) {
     }
     e->it += (unsigned)nt;
     return cuda_rc(cudaGetLastError());
+}
+
+// gpe_evolve_dipolar (dev/gpe_engine.cu:1550-1602), Strang splitting with the
+// dipolar potential recomputed for each half: the density's 3D transform runs
+// as forward axis passes (z, y), the kernel multiply between the forward and
+// inverse x transform, inverse axis passes (y, z); the last inverse pass also
+// applies exp(c3 (Vext(it) + vdip)) and, in the first half, the z kinetic
+// factor.  psi2 holds the transform.  Both halves evaluate Vext at `it`.
+static void dipolar_half(std::vector<PassDesc>& s, uint32_t dens_flags, uint32_t step_flags) {
+    s.push_back({AX_Z, PRE_NONE, DIP_DENS_FWD, POST_NONE, F_DIP | F_STORE | dens_flags, B_PSI, B_PSI2});
+    s.push_back({AX_Y, PRE_NONE, DIP_FWD, POST_NONE, F_DIP | F_STORE, B_PSI2, B_PSI2});
+    s.push_back({AX_X, PRE_NONE, DIP_VDD, POST_NONE, F_DIP | F_STORE, B_PSI2, B_PSI2});
+    s.push_back({AX_Y, PRE_NONE, DIP_INV, POST_NONE, F_DIP | F_STORE, B_PSI2, B_PSI2});
+    if (step_flags) s.push_back({AX_Z, PRE_NONE, DIP_STEP, POST_NONE, F_DIP | F_STORE | step_flags, B_PSI2, B_PSI});
+}
+
+static std::vector<PassDesc> schedule_dipolar(const Engine* e) {
+    std::vector<PassDesc> s;
+    const bool ite = e->beta != 0.0;
+    dipolar_half(s, ite ? F_SCALE_IN : 0u, F_KIN | (ite ? F_SCALE_OPD : 0u));
+    s.push_back({AX_Y, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
+    s.push_back({AX_X, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
+    dipolar_half(s, 0u, F_FIN_STEP | (ite ? F_REDUCE : 0u));
+    return s;
+}
+
+static int evolve_dipolar(Engine* e, int nt, double* mu) {
+    if (nt <= 0) return 0;
+    const std::vector<PassDesc> s = schedule_dipolar(e);
+    e->passes_per_step = (int)s.size();
+    GPE_RC(run_steps(e, s, nt));
+    e->lap_valid = false;
+    if (e->beta != 0.0) {
+        GPE_RC(e->prec == GPE_PRECISION_FP32 ? finish_ite<float>(e) : finish_ite<double>(e));
+        if (mu) {
+            double m = 0.0;
+            GPE_CK(cudaMemcpyAsync(&m, &e->dyn->mu, sizeof(double), cudaMemcpyDeviceToHost, e->st));
+            GPE_CK(cudaStreamSynchronize(e->st));
+            *mu = m;
+        }
+    }
+    e->it += (unsigned)nt;
+    return cuda_rc(cudaGetLastError());
+}
+
+// gpe_energy_dipolar2 (dev/gpe_engine.cu:1789-1809): 1/2 sum rho vdip
+template <typename R>
+static int energy_dipolar(Engine* e, double* edip) {
+    std::vector<PassDesc> s;
+    dipolar_half(s, 0u, 0u);
+    for (const PassDesc& d : s) GPE_RC(launch_desc<R>(e, d));
+    PassArgs<R> a = desc_args<R>(e, {AX_Z, PRE_NONE, DIP_EN, POST_NONE, F_DIP | F_FIN_RED, B_PSI2, B_NONE});
+    a.red_slot = 6;
+    e->launches++;
+    GPE_CK(launch_pass<R>(a, e->n3[AX_Z], AX_Z, pencils_of(e, AX_Z), e->st));
+    GPE_CK(cudaMemcpyAsync(edip, &e->dyn->red[6], sizeof(double), cudaMemcpyDeviceToHost, e->st));
+    GPE_CK(cudaStreamSynchronize(e->st));
+    return 0;
 }
 
 // gpe_evolve_vortex{,2,3} / gpe_evolve_enforced_phase (dev/gpe_engine.cu:1115-1477):
@@ -1279,7 +1346,7 @@ int gpe_gb_create(gpe_gb_engine** out, int nx, int ny, int nz, int interactions,
     if (!out) return GPE_ERR_ARGUMENT;
     *out = nullptr;
     if (!gpe::pow2_side(nx) || !gpe::pow2_side(ny) || !gpe::pow2_side(nz)) return GPE_ERR_LATTICE;
-    if (interactions < -1 || interactions > 1) return GPE_ERR_FUNCTIONAL;
+    if (interactions < -2 || interactions > 1) return GPE_ERR_FUNCTIONAL;
     if (precision != GPE_PRECISION_FP64 && precision != GPE_PRECISION_FP32) return GPE_ERR_ARGUMENT;
     gpe_gb_engine* h = new (std::nothrow) gpe_gb_engine();
     if (!h) return GPE_ERR_ARGUMENT;
@@ -1288,7 +1355,8 @@ int gpe_gb_create(gpe_gb_engine** out, int nx, int ny, int nz, int interactions,
     for (int a = 0; a < 3; a++) e->l3[a] = __builtin_ctz((unsigned)e->n3[a]);
     e->n = (size_t)nx * ny * nz;
     e->inter = interactions;
-    e->gamma = (interactions == -1) ? 1.0 : 2.0;  // GPE_FOR defaults, dev/gpe_user_defined.h:104,182,289
+    // GPE_FOR defaults, dev/gpe_user_defined.h:104,182,289,369
+    e->gamma = (interactions < 0) ? 1.0 : 2.0;
     e->prec = precision;
     e->alpha = alpha; e->beta = beta; e->dt = dt; e->npart = npart;
     e->dt_step = dt;
@@ -1531,6 +1599,24 @@ int gpe_gb_evolve_qf(gpe_gb_engine* h, int nt, double* mu) {
     Engine* e = &h->e;
     GPE_RC(gpe::evolve(e, nt * e->sub, mu));
     return gpe::cuda_rc(cudaStreamSynchronize(e->st));
+}
+
+int gpe_gb_evolve_dipolar(gpe_gb_engine* h, int nt, double* mu) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    Engine* e = &h->e;
+    if (e->inter != gpe::INTER_DIP || e->wz != 0.0) return GPE_ERR_ARGUMENT;
+    GPE_RC(gpe::evolve_dipolar(e, nt, mu));
+    return gpe::cuda_rc(cudaStreamSynchronize(e->st));
+}
+
+int gpe_gb_energy_dipolar(gpe_gb_engine* h, double* t, double* edip) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    if (!edip) return GPE_ERR_ARGUMENT;
+    Engine* e = &h->e;
+    if (e->inter != gpe::INTER_DIP) return GPE_ERR_ARGUMENT;
+    GPE_RC(e->prec == GPE_PRECISION_FP32 ? gpe::energy_dipolar<float>(e, edip) : gpe::energy_dipolar<double>(e, edip));
+    if (t) *t = e->t0 + e->dt * e->it;
+    return 0;
 }
 
 int gpe_gb_energy(gpe_gb_engine* h, double* t, double* ekin, double* eint, double* eext) {

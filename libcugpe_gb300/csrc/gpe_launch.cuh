@@ -52,6 +52,7 @@ cudaError_t launch_ax(const PassArgs<R>& a, size_t pencils, cudaStream_t st, uns
         case C_KIN: return launch_one<R, N, AX, NT, C_KIN>(a, pencils, st);
         case C_EPI: return launch_one<R, N, AX, NT, C_EPI>(a, pencils, st);
         case C_LAP: return launch_one<R, N, AX, NT, C_LAP>(a, pencils, st);
+        case C_DIP: return launch_one<R, N, AX, NT, C_DIP>(a, pencils, st);
         default: return launch_one<R, N, AX, NT, C_EN>(a, pencils, st);
     }
 }

@@ -61,6 +61,16 @@ enum : uint32_t {  // flags
     F_VEXTRA = 1u << 12,    // time-sliced additive potential table
     F_LAP_OUT = 1u << 13,   // after the store: lap = D_a(result) (Laplacian of the new psi)
     F_WZ = 1u << 14,        // Weizsaecker gradient sums of this axis (wg, ws) from D1_a psi
+    F_DIP = 1u << 15,       // dipolar convolution pass (mid = DIP_* mode)
+    F_SCALE_OPD = 1u << 16, // dipolar step: the staged psi is scaled by the pending norm factor
+};
+enum : int {  // dipolar pass modes (in `mid` with F_DIP)
+    DIP_DENS_FWD = 1,  // x = (Gamma |psi|^2, 0), forward FFT_a -> out      (dev/gpe_engine.cu:618-626)
+    DIP_FWD = 2,       // forward FFT_a -> out
+    DIP_VDD = 3,       // forward FFT_a, x gpe_Vpp_k(k)/nxyz, inverse FFT_a (dev/gpe_engine.cu:958-974)
+    DIP_INV = 4,       // inverse FFT_a -> out
+    DIP_STEP = 5,      // inverse FFT_a -> vdip; psi exp(c3 (Vext + dEDF + vdip)) [+ K_a]  (:979-1006)
+    DIP_EN = 6,        // inverse FFT_a -> vdip; partial sums of rho vdip / 2     (:1774-1809)
 };
 
 // Scalars that change while a step runs; they live in device memory so one
@@ -94,6 +104,7 @@ struct PassArgs {
     R* wg;               // Weizsaecker: sum over axes done so far of (d_a rho)^2
     R* ws;               // Weizsaecker: sum over axes done so far of |D1_a psi|^2
     const R* ld1;        // k_a / N_a of this axis (first derivative)
+    const R* kgx; const R* kgy; const R* kgz;  // k grids of the three axes (dipolar kernel)
     const R* vx; const R* vy; const R* vz;   // trap tables
     const R* vextra;     // [slices][n] additive potential (F_VEXTRA)
     int vsteps, vslices;
@@ -123,6 +134,18 @@ template <typename R> __device__ __forceinline__ R vext_at(const PassArgs<R>& a,
 }
 
 template <typename C> __device__ __forceinline__ C ldc(const C* p) { return *p; }
+
+// gpe_Vpp_k / nxyz (dev/gpe_user_defined.h:422-438, dev/gpe_engine.cu:972): Fourier transform of the
+// contact + dipole-dipole pseudopotential, dipoles along z, with the inverse FFT normalisation
+template <typename R> __device__ __forceinline__ R vdd_k(const PassArgs<R>& a, int ix, int iy, int iz) {
+    const R kx = __ldg(a.kgx + ix), ky = __ldg(a.kgy + iy), kz = __ldg(a.kgz + iz);
+    const R k2 = kx * kx + ky * ky + kz * kz;
+    const R fpi = (R)(4.0 * M_PI);
+    R v;
+    if (k2 < (R)2.220446049250313e-16) v = fpi * a.ph.a_scat * (R)1;  // DBL_EPSILON
+    else v = fpi * (a.ph.a_scat * (R)1 + a.ph.a_dip * ((R)3 * kz * kz / k2 - (R)1));
+    return v / a.ph.nxyz;
+}
 
 // Deterministic block sum of the first NR of NRED doubles; result valid in thread 0.
 template <int NT, int NR>
@@ -241,6 +264,7 @@ enum : uint32_t {
 
 __host__ __device__ inline uint32_t staged_ops(int mid, int post, uint32_t flags) {
     uint32_t m = 0;
+    if (flags & F_DIP) return (mid == DIP_STEP || mid == DIP_EN) ? OP_PSI : 0u;
     if (mid == MID_LAP_ACC) m |= OP_LAP;
     if (mid == MID_QF_VSTEP1) m |= OP_LAP | OP_COPY;
     if (mid == MID_CURRENT) m |= OP_COPY;
@@ -322,10 +346,11 @@ struct PassGeom {
 
 // Kernel classes: each instantiation compiles only the code its passes use,
 // which keeps register use and instruction footprint down.
-enum : int { C_KIN = 0, C_EPI = 1, C_LAP = 2, C_EN = 3 };
+enum : int { C_KIN = 0, C_EPI = 1, C_LAP = 2, C_EN = 3, C_DIP = 4 };
 
 __host__ __device__ inline int op_class(int pre, int mid, int post, uint32_t flags) {
     (void)mid;
+    if (flags & F_DIP) return C_DIP;
     if (flags & F_EKIN) return C_EN;
     if (flags & F_LAP) return C_LAP;
     if (pre != PRE_NONE || post != POST_NONE ||
@@ -341,7 +366,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     using Geo = PassGeom<R, N, AX, NT>;
     constexpr int E = Geo::E, T = Geo::T, CW = Geo::CW, G = Geo::G, W = Geo::W, ROW = Geo::ROW;
     constexpr int SSTR = (AX == AX_Z) ? 1 : CW;
-    constexpr bool FIN = (CLS == C_EPI || CLS == C_EN);
+    constexpr bool FIN = (CLS == C_EPI || CLS == C_EN || CLS == C_DIP);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C2<R>* stw = reinterpret_cast<C2<R>*>(smem_raw);
     C2<R>* skt = stw + Geo::TW;
@@ -410,7 +435,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     C2<R>* slotB = nullptr;
     R* slotC = nullptr;
     R* slotD = nullptr;
-    if constexpr (CLS == C_EPI || CLS == C_LAP) {
+    if constexpr (CLS == C_EPI || CLS == C_LAP || CLS == C_DIP) {
         ops = staged_ops(a.mid, a.post, a.flags);
         unsigned char* sop = smem_raw + Geo::SMEM_BASE;
         slotA = reinterpret_cast<C2<R>*>(sop);
@@ -536,6 +561,66 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                 own(q) = v;
             }
             from_cells();
+        }
+    }
+
+    // ------------------------------------------ dipolar convolution (C_DIP)
+    if constexpr (CLS == C_DIP) {
+        const int dm = a.mid;
+        if (dm == DIP_DENS_FWD) {
+#pragma unroll
+            for (int q = 0; q < E; q++) x[q] = mk<R>(density(a.ph, x[q]), (R)0);
+        }
+        if (dm == DIP_DENS_FWD || dm == DIP_FWD || dm == DIP_VDD) fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
+        if (dm == DIP_VDD) {
+#pragma unroll
+            for (int q = 0; q < E; q++) {
+                int ix, iy, iz;
+                decode(at(q), ix, iy, iz);
+                x[q] = cscale(x[q], vdd_k(a, ix, iy, iz));
+            }
+        }
+        if (dm != DIP_DENS_FWD && dm != DIP_FWD) fft<R, N, true, SSTR, G>(x, sb, t, stw, bar);
+        if (dm == DIP_STEP || dm == DIP_EN) {
+            cp_async_wait_all();
+            if (valid) {
+                const bool sc = (a.flags & F_SCALE_OPD) != 0;
+                to_cells();
+#pragma unroll 1
+                for (int q = 0; q < E; q++) {
+                    const uint32_t idx = at(q);
+                    int ix, iy, iz;
+                    decode(idx, ix, iy, iz);
+                    const R vdip = own(q).x;  // real part of the convolution (dev/gpe_engine.cu:997-998)
+                    C2<R> p = slotA[q * NT + tid];
+                    if (sc) p = cscale(p, s_prev);
+                    const R rho = density(a.ph, p);
+                    if (dm == DIP_EN) {
+                        acc[0] += 0.5 * (double)rho * (double)vdip;
+                        own(q) = p;
+                    } else {
+                        const R V = (vext_at(a, idx, ix, iy, iz, it) + dEDFdn(a.ph, rho)) + vdip;
+                        own(q) = cmul(p, phase(a.ph, V));
+                    }
+                }
+                from_cells();
+            }
+            if (dm == DIP_STEP && (a.flags & F_KIN)) {
+                fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
+#pragma unroll
+                for (int q = 0; q < E; q++) x[q] = cmul(x[q], skt[t + T * q]);
+                fft<R, N, true, SSTR, G>(x, sb, t, stw, bar);
+            }
+            if (a.flags & F_REDUCE) {
+                if constexpr (sizeof(R) == 4) {
+#pragma unroll
+                    for (int q = 0; q < E; q++) nff = ff_add(nff, a.ph.gamma * (x[q].x * x[q].x + x[q].y * x[q].y));
+                } else {
+#pragma unroll
+                    for (int q = 0; q < E; q++)
+                        acc[0] += (double)a.ph.gamma * ((double)x[q].x * (double)x[q].x + (double)x[q].y * (double)x[q].y);
+                }
+            }
         }
     }
 
@@ -695,10 +780,14 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
         if (a.flags & (F_FIN_S2 | F_FIN_STEP | F_FIN_RED)) {
             // energy: 3 sums; norm: 1; a real-time step only advances the step counter
             constexpr int NR = (CLS == C_EN) ? 3 : 1;
-            const bool sums = (CLS == C_EN) || (a.flags & F_REDUCE);
+            const bool sums = (CLS == C_EN) || (a.flags & (F_REDUCE | F_FIN_RED));
             if (sums) {
-                if constexpr (CLS == C_EPI && sizeof(R) == 4) acc[0] = block_sum_ff<NT>(nff, sred);
-                else block_sum<NT, NR>(acc, sred);
+                if constexpr ((CLS == C_EPI || CLS == C_DIP) && sizeof(R) == 4) {
+                    if (a.flags & F_REDUCE) acc[0] = block_sum_ff<NT>(nff, sred);
+                    else block_sum<NT, NR>(acc, sred);
+                } else {
+                    block_sum<NT, NR>(acc, sred);
+                }
             }
             if (tid == 0) {
                 if (sums)

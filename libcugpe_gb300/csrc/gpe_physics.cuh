@@ -8,6 +8,8 @@
 //   gpe_dEDFdn / gpe_EDF   dev/gpe_user_defined.h:118-135   unitary Fermi gas (INTERACTIONS 0)
 //                          dev/gpe_user_defined.h:196-243   BEC side of the crossover (1)
 //                          dev/gpe_user_defined.h:305-322   contact BEC (-1)
+//                          dev/gpe_user_defined.h:380-438   dipolar BEC (-2): local part 0, contact and
+//                                                           dipolar parts in the k-space kernel
 //   cplxExp(c3 * V)        dev/gpe_complex.cuh:167-175, dev/gpe_engine.cu:738
 // The trap is tabulated per axis on the host, V(ix,iy,iz) = vx[ix] + vy[iy]
 // + vz[iz], with the same evaluation order as the reference expression.
@@ -18,7 +20,7 @@
 
 namespace gpe {
 
-enum : int { INTER_BEC = -1, INTER_UFG = 0, INTER_BECSIDE = 1 };
+enum : int { INTER_DIP = -2, INTER_BEC = -1, INTER_UFG = 0, INTER_BECSIDE = 1 };
 enum : int { PHASE_GENERAL = 0, PHASE_ROTATE = 1, PHASE_DECAY = 2 };
 
 // 3 pi^2 as the reference's left-to-right constant fold (3.0*M_PI)*M_PI
@@ -36,6 +38,8 @@ struct Phys {
     R qf_g;           // quantum friction coefficient / Gamma
     R wz8;            // Weizsaecker weight / 8
     R wz_eps;         // density regularisation of the Weizsaecker potential
+    R a_dip;          // dipolar length (user param A_DIP, INTERACTIONS -2)
+    R nxyz;           // lattice points (FFT normalisation of the dipolar kernel)
 };
 
 __device__ __forceinline__ double gexp(double x) { return exp(x); }
@@ -54,6 +58,7 @@ template <typename R> __device__ __forceinline__ R density(const Phys<R>& p, C2<
 // variational derivative of the energy density functional
 template <typename R> __device__ __forceinline__ R dEDFdn(const Phys<R>& p, R rho) {
     if (p.inter == INTER_BEC) return p.c_bec * rho;
+    if (p.inter == INTER_DIP) return (R)0;  // dev/gpe_user_defined.h:400-404
     if (p.inter == INTER_UFG) {
         // 0.37 (3 pi^2 rho)^{2/3} / 2 ; (x^{1/3})^2 replaces pow(x, 2/3)
         const R t = gcbrt((R)GPE_3PI2 * rho);
@@ -75,7 +80,7 @@ template <typename R> __device__ __forceinline__ R dEDFdn(const Phys<R>& p, R rh
 
 // energy density functional (only used by the energy reduction, in FP64)
 __device__ __forceinline__ double EDF(const Phys<double>& p, double rho) {
-    if (p.inter == INTER_BEC) return 0.5 * p.c_bec * rho * rho;  // 2 pi a rho^2
+    if (p.inter == INTER_BEC || p.inter == INTER_DIP) return 0.5 * p.c_bec * rho * rho;  // 2 pi a rho^2
     if (p.inter == INTER_UFG) return 0.37 * 0.6 * rho * pow(GPE_3PI2 * rho, 2.0 / 3.0) / 2.;
     const double XI = 0.37, CT = 0.901, a = p.a_scat;
     const double kF = cbrt(GPE_3PI2 * rho);

@@ -22,7 +22,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libgpe_oracle.so")
 
-INTER_GAMMA = {-1: 1.0, 0: 2.0, 1: 2.0}
+INTER_GAMMA = {-2: 1.0, -1: 1.0, 0: 2.0, 1: 2.0}
 
 
 def build(force: bool = False) -> str:
@@ -72,6 +72,10 @@ def lib():
         L.oracle_energy.restype = i
         L.oracle_get_currents.argtypes = [vp, dp, dp, dp, dp]
         L.oracle_set_wz.argtypes = [vp, d, d]
+        L.oracle_evolve_dipolar.argtypes = [vp, i, dp]
+        L.oracle_evolve_dipolar.restype = i
+        L.oracle_energy_dipolar.argtypes = [vp]
+        L.oracle_energy_dipolar.restype = d
         L.oracle_wz_potential.argtypes = [vp, dp]
         L.oracle_get_currents.restype = i
         L.oracle_fft3d.argtypes = [i, i, i, dp, i, i]
@@ -143,6 +147,14 @@ class Oracle:
         t = ctypes.c_double()
         lib().oracle_get_density(self._h, ctypes.byref(t), _dp(out))
         return t.value, out
+
+    def evolve_dipolar(self, nt):
+        mu = ctypes.c_double(0.0)
+        lib().oracle_evolve_dipolar(self._h, int(nt), ctypes.byref(mu))
+        return mu.value
+
+    def energy_dipolar(self):
+        return lib().oracle_energy_dipolar(self._h)
 
     def set_weizsacker(self, lam, eps=0.0):
         lib().oracle_set_wz(self._h, float(lam), float(eps))

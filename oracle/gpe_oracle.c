@@ -29,6 +29,7 @@
  * problem): an optional additive potential table, one real field per time
  * slice, selected by it / steps_per_slice.
  */
+#include <float.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -203,6 +204,7 @@ static inline double vext(const gpe_oracle *o, size_t idx, int ix, int iy, int i
 static inline double dEDFdn(const gpe_oracle *o, double rho) {
     if (o->inter == 0) return 0.37 * pow(3.0 * M_PI * M_PI * rho, 2.0 / 3.0) / 2.0;
     if (o->inter == -1) { const double a = o->up[3]; return 4 * M_PI * a * rho; }
+    if (o->inter == -2) return 0.0; /* dipolar BEC: dev/gpe_user_defined.h:400-404 */
     if (o->inter == 1) {
         const double a = o->up[3];
         if (rho > 1e-15) {
@@ -221,7 +223,7 @@ static inline double dEDFdn(const gpe_oracle *o, double rho) {
 
 static inline double EDF(const gpe_oracle *o, double rho) {
     if (o->inter == 0) return 0.37 * 0.6 * rho * pow(3.0 * M_PI * M_PI * rho, 2.0 / 3.0) / 2.;
-    if (o->inter == -1) { const double a = o->up[3]; return 2 * M_PI * a * rho * rho; }
+    if (o->inter == -1 || o->inter == -2) { const double a = o->up[3]; return 2 * M_PI * a * rho * rho; }
     if (o->inter == 1) {
         const double a = o->up[3];
         const double kF = pow(3.0 * M_PI * M_PI * rho, 1.0 / 3.0);
@@ -679,6 +681,77 @@ int oracle_get_currents(void *h, double *t, double *jx, double *jy, double *jz) 
         for (long i = 0; i < n; i++) out[a][i] = o->psi[i].x * o->wrk3C[i].x + o->psi[i].y * o->wrk3C[i].y;
     }
     return 0;
+}
+
+/* dipolar potential of psi: FFT of (rho, 0) (dev/gpe_engine.cu:618-626), times
+ * gpe_Vpp_k / nxyz (dev/gpe_user_defined.h:422-438, dev/gpe_engine.cu:958-974),
+ * inverse FFT, real part (:997-998) */
+static void vdip_field(gpe_oracle *o, const cd *psi, double *vdip) {
+    const int ny = o->ny, nz = o->nz;
+    const long n = (long)o->n;
+    const double a_con = o->up[3], a_dip = o->up[4];
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+    for (long i = 0; i < n; i++) { o->wrk3C[i].x = density(o, psi[i]); o->wrk3C[i].y = 0.0; }
+    fft3d(o, o->wrk3C, -1);
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+    for (long i = 0; i < n; i++) {
+        DECODE((size_t)i);
+        const double kx = o->kx[ix], ky = o->ky[iy], kz = o->kz[iz];
+        const double k_sq = kx * kx + ky * ky + kz * kz;
+        const double v = (k_sq < DBL_EPSILON) ? 4. * M_PI * a_con * 1.0
+                                              : 4. * M_PI * (a_con * 1.0 + a_dip * (3. * kz * kz / k_sq - 1.));
+        o->wrk3C[i] = cscale(o->wrk3C[i], v / (double)o->n);
+    }
+    fft3d(o, o->wrk3C, +1);
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+    for (long i = 0; i < n; i++) vdip[i] = o->wrk3C[i].x;
+}
+
+/* exp(c3 (Vext(it) + dEDF + vdip)) psi (dev/gpe_engine.cu:979-1006) */
+static void dipolar_vstep(gpe_oracle *o, unsigned it) {
+    const int ny = o->ny, nz = o->nz;
+    const long n = (long)o->n;
+    vdip_field(o, o->psi, o->V);
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+    for (long i = 0; i < n; i++) {
+        DECODE((size_t)i);
+        const cd lpsi = o->psi[i];
+        const double lrho = density(o, lpsi);
+        const double lv = vext(o, (size_t)i, ix, iy, iz, it) + dEDFdn(o, lrho) + o->V[i];
+        o->psi[i] = cmul(lpsi, cexp_(cscale(o->c3, lv)));
+    }
+}
+
+/* gpe_evolve_dipolar (dev/gpe_engine.cu:1550-1602) */
+int oracle_evolve_dipolar(void *h, int nt, double *mu) {
+    gpe_oracle *o = (gpe_oracle *)h;
+    for (int step = 0; step < nt; step++) {
+        const unsigned it = o->it;
+        dipolar_vstep(o, it);
+        fft3d(o, o->psi, -1);
+        mult_expT(o, o->psi);
+        fft3d(o, o->psi, +1);
+        dipolar_vstep(o, it);
+        if (o->beta != 0.0) {
+            const double norm = normalize(o, o->psi);
+            if (mu) *mu = -.5 * log(norm / o->npart) / o->dt;
+        }
+        o->it = o->it + 1;
+    }
+    return 0;
+}
+
+/* gpe_energy_dipolar2 (dev/gpe_engine.cu:1789-1809): 1/2 sum rho vdip */
+double oracle_energy_dipolar(void *h) {
+    gpe_oracle *o = (gpe_oracle *)h;
+    const long n = (long)o->n;
+    vdip_field(o, o->psi, o->V);
+    double *w = (double *)malloc(sizeof(double) * n);
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+    for (long i = 0; i < n; i++) w[i] = density(o, o->psi[i]) * o->V[i];
+    const double e = 0.5 * det_sum(o, w);
+    free(w);
+    return e;
 }
 
 /* raw 3D transform, exposed so the tests can pin the restated FFT against numpy */

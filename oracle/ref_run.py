@@ -35,13 +35,15 @@ def run(shape, interactions, alpha, beta, dt, npart, params, psi0, cmds, qf=0.0,
         r = subprocess.run(args, capture_output=True, text=True, timeout=timeout)
         if r.returncode != 0:
             raise RuntimeError(f"reference run failed ({r.returncode}): {r.stderr[-2000:]}")
-        out = {"psi": [], "energy": [], "mu": [], "time_ms": [], "t": [], "currents": []}
+        out = {"psi": [], "energy": [], "mu": [], "time_ms": [], "t": [], "currents": [], "edip": []}
         for line in r.stdout.splitlines():
             f = line.split()
             if not f:
                 continue
             if f[0] == "E":
                 out["energy"].append(tuple(float(x) for x in f[1:5]))
+            elif f[0] == "W":
+                out["edip"].append(float(f[2]))
             elif f[0] == "MU":
                 out["mu"].append(float(f[1]))
             elif f[0] == "TIME":

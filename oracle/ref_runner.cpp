@@ -22,6 +22,10 @@
 //     G      gpe_get_phase(NULL)
 //     P<k>   gpe_evolve_enforced_phase(k, &mu) -> "MU mu"
 //     J      gpe_get_currents() -> OUTDIR/cur_<i>.bin (jx, jy, jz), "J t"
+//     A<x>   fifth user parameter (A_DIP of the dipolar functional) = x, gpe_set_user_params(5, .)
+//     Y<k>   gpe_evolve_dipolar(k, &mu) -> "MU mu"
+//     W      gpe_energy_dipolar2() -> "W t edip"  (gpe_energy_dipolar itself indexes -k past the
+//            transform for the k = 0 planes, dev/gpe_engine.cu:1725, and is not called)
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -37,7 +41,7 @@ int main(int argc, char** argv) {
     std::string outdir = argv[2];
     double alpha = atof(argv[3]), beta = atof(argv[4]), dt = atof(argv[5]);
     double npart = atof(argv[6]), qf = atof(argv[7]);
-    double params[4] = {atof(argv[8]), atof(argv[9]), atof(argv[10]), atof(argv[11])};
+    double params[5] = {atof(argv[8]), atof(argv[9]), atof(argv[10]), atof(argv[11]), 0.0};
     std::string cmds = argv[12];
 
     int nx, ny, nz;
@@ -121,6 +125,17 @@ int main(int argc, char** argv) {
             fwrite(j.data(), sizeof(double), 3 * n, g);
             fclose(g);
             printf("J %.17g\n", t);
+        } else if (c[0] == 'A') {
+            params[4] = atof(c.c_str() + 1);
+            CHECK(gpe_set_user_params(5, params));
+        } else if (c[0] == 'Y') {
+            double mu = 0.0;
+            CHECK(gpe_evolve_dipolar(atoi(c.c_str() + 1), &mu));
+            printf("MU %.17g\n", mu);
+        } else if (c == "W") {
+            double t = 0.0, ed = 0.0;
+            CHECK(gpe_energy_dipolar2(&t, &ed));
+            printf("W %.17g %.17g\n", t, ed);
         } else if (c == "G") {
             CHECK(gpe_get_phase(NULL));
         } else if (c[0] == 'P') {

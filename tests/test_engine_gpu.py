@@ -296,3 +296,50 @@ def test_weizsacker_substeps_keep_the_step_length(cuda_device, gpe_lib):
     o.evolve_qf(4)
     assert e.get_psi()[0] == pytest.approx(0.5)
     assert rel(e.get_psi()[1], o.get_psi()[1]) <= 1e-11
+
+
+DIP_PARAMS = [0.0625, 0.0625, 0.05, 2.0, 1.5]  # OMEGA_X..Z, A_CON, A_DIP
+
+
+def make_dip_pair(shape, alpha, beta, precision=g.FP64, seed=31):
+    psi = configs.random_state(shape, seed=seed, npart=1.0, gamma=1.0)
+    e = g.Engine(shape, -2, alpha, beta, 0.05, 1.0, precision=precision)
+    e.set_user_params(DIP_PARAMS)
+    e.set_psi(0.0, psi)
+    o = oracle.Oracle(shape, -2, alpha, beta, 0.05, 1.0, threads=4)
+    o.set_user_params(DIP_PARAMS)
+    o.set_psi(0.0, psi)
+    return e, o
+
+
+@pytest.mark.parametrize("ab", [(1.0, 0.0), (0.0, 1.0)], ids=["rte", "ite"])
+@pytest.mark.parametrize("shape", [(16, 16, 16), (32, 16, 8), (8, 32, 64)])
+def test_dipolar_fp64_per_step_parity(cuda_device, gpe_lib, shape, ab):
+    """gpe_evolve_dipolar: density transform as axis passes, kernel multiply in the x pass, potential
+    step fused into the last inverse pass; <= 1e-12 per step against the oracle, mu, E_dip."""
+    e, o = make_dip_pair(shape, *ab)
+    for step in range(3):
+        mu_e = e.evolve_dipolar(1)
+        mu_o = o.evolve_dipolar(1)
+        t, po = o.get_psi()
+        assert rel(e.get_psi()[1], po) <= TOL_FP64_STEP, (step, rel(e.get_psi()[1], po))
+        if ab[1] != 0.0:
+            assert abs(mu_e - mu_o) <= 1e-10 * max(1.0, abs(mu_o))
+        e.set_psi(t, po)
+        o.set_psi(t, po)
+    assert e.energy_dipolar()[1] == pytest.approx(o.energy_dipolar(), rel=1e-12)
+    e.evolve_dipolar(10)
+    o.evolve_dipolar(10)
+    assert rel(e.get_psi()[1], o.get_psi()[1]) <= 2e-11
+    assert e.get_psi()[0] == pytest.approx(o.get_psi()[0])
+
+
+def test_dipolar_fp32_against_fp64_oracle(cuda_device, gpe_lib):
+    e, o = make_dip_pair((32, 16, 16), 1.0, 0.0, precision=g.FP32)
+    e.evolve_dipolar(1)
+    o.evolve_dipolar(1)
+    assert rel(e.get_psi()[1], o.get_psi()[1]) <= TOL_FP32_STEP
+    e.evolve_dipolar(20)
+    o.evolve_dipolar(20)
+    assert rel(e.get_psi()[1], o.get_psi()[1]) <= 20 * TOL_FP32_STEP
+    assert e.energy_dipolar()[1] == pytest.approx(o.energy_dipolar(), rel=1e-5)

@@ -228,3 +228,28 @@ def test_oracle_weizsacker_potential_gaussian_and_numpy():
     inv = 1.0 / (rho + eps)
     ref = lam / 8 * (grad2 * inv ** 2 - 2 * lrho * inv)
     assert rel(vw, ref) < 1e-12
+
+
+def test_oracle_dipolar_potential_and_energy():
+    """gpe_evolve_dipolar's potential (dev/gpe_engine.cu:958-1006): with a_dip = 0 the kernel is the
+    contact term 4 pi a, so E_dip = 2 pi a sum rho^2; with a_dip != 0 the energy matches a numpy
+    restatement of 1/2 sum rho IFFT(Vpp(k) FFT rho / n)."""
+    shape, a_con, a_dip = (16, 8, 32), 2.0, 1.5
+    psi = configs.random_state(shape, seed=17, npart=1.0, gamma=1.0)
+    rho = np.abs(psi) ** 2
+    o = oracle.Oracle(shape, -2, 1.0, 0.0, 0.05, 1.0, threads=2)
+    o.set_user_params([0.06, 0.06, 0.05, a_con, 0.0])
+    o.set_psi(0.0, psi)
+    assert o.energy_dipolar() == pytest.approx(2 * np.pi * a_con * np.sum(rho ** 2), rel=1e-12)
+    o.set_user_params([0.06, 0.06, 0.05, a_con, a_dip])
+    k = [2 * np.pi * np.fft.fftfreq(n) for n in shape]
+    KX, KY, KZ = np.meshgrid(*k, indexing="ij")
+    k2 = KX ** 2 + KY ** 2 + KZ ** 2
+    with np.errstate(divide="ignore", invalid="ignore"):
+        vk = np.where(k2 < np.finfo(float).eps, 4 * np.pi * a_con, 4 * np.pi * (a_con + a_dip * (3 * KZ ** 2 / k2 - 1)))
+    vdip = np.real(np.fft.ifftn(vk * np.fft.fftn(rho)))
+    assert o.energy_dipolar() == pytest.approx(0.5 * np.sum(rho * vdip), rel=1e-12)
+    # ITE with the dipolar step keeps the norm and returns mu
+    o.change_alpha_beta(0.0, 1.0)
+    mu = o.evolve_dipolar(3)
+    assert np.isfinite(mu) and o.get_norm() == pytest.approx(1.0, rel=1e-13)

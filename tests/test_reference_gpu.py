@@ -141,3 +141,24 @@ def test_currents_match_reference(reference, gpe_lib, case):
     _, jx, jy, jz = e.get_currents()
     for ours, ref in zip((jx, jy, jz), out["currents"][0]):
         assert rel(ours, ref) <= 1e-12, rel(ours, ref)
+
+
+@pytest.mark.parametrize("ab", [(1.0, 0.0), (0.0, 1.0)], ids=["rte", "ite"])
+def test_dipolar_matches_reference(reference, gpe_lib, ab):
+    """gpe_evolve_dipolar and gpe_energy_dipolar2 of the reference built with INTERACTIONS=-2."""
+    shape = (16, 16, 16)
+    build_ref.build([(16, 16, 16, -2)])
+    params = [0.0625, 0.0625, 0.05, 2.0]
+    psi = configs.random_state(shape, seed=25, npart=1.0, gamma=1.0)
+    out = ref_run.run(shape, -2, ab[0], ab[1], 0.05, 1.0, params, psi, ["A1.5", "W", "Y1", "D", "Y4", "W", "D"])
+    e = g.Engine(shape, -2, ab[0], ab[1], 0.05, 1.0)
+    e.set_user_params(params + [1.5])
+    e.set_psi(0.0, psi)
+    assert e.energy_dipolar()[1] == pytest.approx(out["edip"][0], rel=1e-12)
+    mu = e.evolve_dipolar(1)
+    assert rel(e.get_psi()[1], out["psi"][0]) <= 1e-12
+    if ab[1] != 0.0:
+        assert abs(mu - out["mu"][0]) <= 1e-10 * max(1.0, abs(out["mu"][0]))
+    e.evolve_dipolar(4)
+    assert rel(e.get_psi()[1], out["psi"][1]) <= 1e-11
+    assert e.energy_dipolar()[1] == pytest.approx(out["edip"][1], rel=1e-11)
