@@ -15,9 +15,9 @@
  * lattice comes from gpe_configure() or the GPE_NX/GPE_NY/GPE_NZ/
  * GPE_INTERACTIONS/GPE_PRECISION environment variables.
  *
- * Entry points of the reference outside the split-step evolution (vortex
- * imprinting, phase enforcing, currents, dipolar) are declared so drivers
- * link, and return GPE_ERR_NOT_IMPLEMENTED (-98).
+ * The reference's other evolution and observable entry points (vortex
+ * imprinting, phase enforcing, currents, dipolar evolution and energy) are
+ * implemented on the same engine.
  */
 #ifndef GPE_ENGINE_GB300_DROPIN_H
 #define GPE_ENGINE_GB300_DROPIN_H

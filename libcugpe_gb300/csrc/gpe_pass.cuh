@@ -695,7 +695,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     }
 
     // ---------------------------------------------------------- kinetic pair
-    if constexpr (CLS != C_EN) {
+    if constexpr (CLS != C_EN && CLS != C_DIP) {  // the dipolar passes run their own transforms
         if (CLS != C_LAP || (a.flags & F_KIN)) {
             fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
 #pragma unroll
