@@ -36,8 +36,12 @@ typedef cuDoubleComplex cuCplx;
 #define CUDA_ERRORS_BASE 0
 #define CUFFT_ERRORS_BASE 100
 
-/* user parameter slots (dev/gpe_user_defined.h:101) */
+/* user parameter slots (dev/gpe_user_defined.h:101; dipolar BEC :366) */
+#if defined(INTERACTIONS) && (INTERACTIONS == -2)
+typedef enum { OMEGA_X, OMEGA_Y, OMEGA_Z, A_CON, A_DIP } user_params_t;
+#else
 typedef enum { OMEGA_X, OMEGA_Y, OMEGA_Z, A_SCAT } user_params_t;
+#endif
 
 static inline const char* gpe_get_error_string(gpe_result_t r) { return gpe_gb_error_string(r); }
 
