@@ -53,6 +53,12 @@ cudaError_t launch_ax(const PassArgs<R>& a, size_t pencils, cudaStream_t st, uns
         case C_EPI: return launch_one<R, N, AX, NT, C_EPI>(a, pencils, st);
         case C_LAP: return launch_one<R, N, AX, NT, C_LAP>(a, pencils, st);
         case C_DIP: return launch_one<R, N, AX, NT, C_DIP>(a, pencils, st);
+        case C_EPI_D:
+            if constexpr (sizeof(R) == 4 && N <= 128) return launch_one<R, N, AX, NT, C_EPI_D>(a, pencils, st);
+            else return cudaErrorInvalidValue;
+        case C_LAP_D:
+            if constexpr (sizeof(R) == 4 && N <= 128) return launch_one<R, N, AX, NT, C_LAP_D>(a, pencils, st);
+            else return cudaErrorInvalidValue;
         default: return launch_one<R, N, AX, NT, C_EN>(a, pencils, st);
     }
 }

@@ -63,6 +63,7 @@ enum : uint32_t {  // flags
     F_WZ = 1u << 14,        // Weizsaecker gradient sums of this axis (wg, ws) from D1_a psi
     F_DIP = 1u << 15,       // dipolar convolution pass (mid = DIP_* mode)
     F_SCALE_OPD = 1u << 16, // dipolar step: the staged psi is scaled by the pending norm factor
+    F_DIRECT = 1u << 17,    // psi, V, V_qf, lap and the psi copy are read where used, not staged
 };
 enum : int {  // dipolar pass modes (in `mid` with F_DIP)
     DIP_DENS_FWD = 1,  // x = (Gamma |psi|^2, 0), forward FFT_a -> out      (dev/gpe_engine.cu:618-626)
@@ -276,6 +277,7 @@ __host__ __device__ inline uint32_t staged_ops(int mid, int post, uint32_t flags
     if (post == POST_PART12 && (flags & F_QF)) m |= OP_VQF;
     if (post == POST_PART1) m |= OP_V;
     if (post == POST_VSTEP3) m |= (flags & F_AUX_CPLX) ? OP_AUXC : OP_AUXR;
+    if (flags & F_DIRECT) m &= ~(OP_PSI | OP_V | OP_VQF | OP_LAP | OP_COPY);
     return m;
 }
 
@@ -338,11 +340,11 @@ struct PassGeom {
     // dynamic shared memory cap: the 227 KiB per-CTA opt-in limit less room for the static arrays
     static constexpr size_t SMEM_CAP = 225 * 1024;
     static constexpr size_t SMEM_MAX = SMEM_FULL < SMEM_CAP ? SMEM_FULL : SMEM_CAP;
-    // resident threads per SM the register allocation aims for: FP32 pencils up to 256 points fit
-    // 7 CTAs of 128 threads in 72 registers without spills, which runs the 128^3 and 256^3 passes
-    // (1-2 waves of CTAs) in fewer rounds (measured: +8% RTE, +20% ITE steps/s at 128^3); the
-    // 512-point passes were faster with 4
-    static constexpr int THREADS_SM = (sizeof(R) == 4) ? (N <= 256 ? 896 : 512) : 256;
+    // resident threads per SM the register allocation aims for: FP32 pencils up to 128 points fit
+    // 7 CTAs of 128 threads in 72 registers without spills, 256-point ones 6 in 80, which runs the
+    // 128^3 and 256^3 passes (1-2 waves of CTAs) in fewer rounds (measured: +8% RTE, +20% ITE
+    // steps/s at 128^3, +2% / +16% at 256^3); the 512-point passes were faster with 4
+    static constexpr int THREADS_SM = (sizeof(R) == 4) ? (N <= 128 ? 896 : N <= 256 ? 768 : 512) : 256;
     static constexpr int MINB = (THREADS_SM / NT) > 0 ? THREADS_SM / NT : 1;
     static_assert(NT % G == 0 && NT % 32 == 0, "threads per CTA must hold whole groups");
     static_assert(SMEM_BASE + 2 * (size_t)E * NT * sizeof(C2<R>) <= SMEM_CAP,
@@ -351,16 +353,18 @@ struct PassGeom {
 
 // Kernel classes: each instantiation compiles only the code its passes use,
 // which keeps register use and instruction footprint down.
-enum : int { C_KIN = 0, C_EPI = 1, C_LAP = 2, C_EN = 3, C_DIP = 4 };
+enum : int { C_KIN = 0, C_EPI = 1, C_LAP = 2, C_EN = 3, C_DIP = 4, C_EPI_D = 5, C_LAP_D = 6 };
+// C_EPI_D / C_LAP_D: the epilogue and Laplacian classes reading their operands where used (F_DIRECT),
+// compiled separately so the staged variants keep their register allocation.
 
 __host__ __device__ inline int op_class(int pre, int mid, int post, uint32_t flags) {
     (void)mid;
     if (flags & F_DIP) return C_DIP;
     if (flags & F_EKIN) return C_EN;
-    if (flags & F_LAP) return C_LAP;
+    if (flags & F_LAP) return (flags & F_DIRECT) ? C_LAP_D : C_LAP;
     if (pre != PRE_NONE || post != POST_NONE ||
         (flags & (F_LAP_OUT | F_REDUCE | F_FIN_STEP | F_FIN_S2 | F_FIN_RED)))
-        return C_EPI;
+        return (flags & F_DIRECT) ? C_EPI_D : C_EPI;
     return C_KIN;
 }
 
@@ -368,10 +372,12 @@ __host__ __device__ inline int op_class(int pre, int mid, int post, uint32_t fla
 // working on it (a standalone launch, or one condensate of a batch).
 template <typename R, int N, int AX, int NT, int CLS>
 __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, uint32_t nblk) {
+    constexpr bool DIRECT = (CLS == C_EPI_D || CLS == C_LAP_D);
+    constexpr int K = (CLS == C_EPI_D) ? C_EPI : (CLS == C_LAP_D) ? C_LAP : CLS;  // base class
     using Geo = PassGeom<R, N, AX, NT>;
     constexpr int E = Geo::E, T = Geo::T, CW = Geo::CW, G = Geo::G, W = Geo::W, ROW = Geo::ROW;
     constexpr int SSTR = (AX == AX_Z) ? 1 : CW;
-    constexpr bool FIN = (CLS == C_EPI || CLS == C_EN || CLS == C_DIP);
+    constexpr bool FIN = (K == C_EPI || K == C_EN || K == C_DIP);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C2<R>* stw = reinterpret_cast<C2<R>*>(smem_raw);
     C2<R>* skt = stw + Geo::TW;
@@ -382,10 +388,10 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
 
     const int tid = threadIdx.x;
     for (int i = tid; i < Geo::TW; i += NT) stw[i] = a.tw[i];
-    if constexpr (CLS != C_EN) {
+    if constexpr (K != C_EN) {
         for (int i = tid; i < N; i += NT) skt[i] = a.ktab[i];
     }
-    if constexpr (CLS != C_KIN) {
+    if constexpr (K != C_KIN) {
         for (int i = tid; i < N; i += NT) slt[i] = a.ltab[i];
     }
 
@@ -440,7 +446,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     C2<R>* slotB = nullptr;
     R* slotC = nullptr;
     R* slotD = nullptr;
-    if constexpr (CLS == C_EPI || CLS == C_LAP || CLS == C_DIP) {
+    if constexpr (K == C_EPI || K == C_LAP || K == C_DIP) {
         ops = staged_ops(a.mid, a.post, a.flags);
         unsigned char* sop = smem_raw + Geo::SMEM_BASE;
         slotA = reinterpret_cast<C2<R>*>(sop);
@@ -482,6 +488,18 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     // so their transcendental-heavy bodies appear once in the instruction
     // stream instead of E times.
     auto own = [&](int q) -> C2<R>& { return sb[padp(t + T * q) * SSTR]; };
+    // operands of the MID/POST ops: staged in shared memory, or read where used (F_DIRECT: frees the
+    // slots' shared memory for more resident CTAs where the transforms are short)
+    constexpr bool direct = DIRECT;
+    auto op_psi = [&](int q, uint32_t idx) -> C2<R> { return direct ? a.psi[idx] : slotA[q * NT + tid]; };
+    auto op_lap = [&](int q, uint32_t idx) -> C2<R> { return direct ? a.lap[idx] : slotA[q * NT + tid]; };
+    auto op_v = [&](int q, uint32_t idx) -> R { return direct ? a.V[idx] : slotC[q * NT + tid]; };
+    auto op_vqf = [&](int q, uint32_t idx) -> R { return direct ? a.Vqf[idx] : slotD[q * NT + tid]; };
+    auto op_copy = [&](int q, uint32_t idx) -> C2<R> {  // the loaded (and scaled) psi
+        if (!direct) return slotB[q * NT + tid];
+        const C2<R> p = a.in[idx];
+        return scale_in ? cscale(p, s_prev) : p;
+    };
     auto to_cells = [&]() {
 #pragma unroll
         for (int q = 0; q < E; q++) own(q) = x[q];
@@ -529,7 +547,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     (void)wz_grad;
 
     // ---------------------------------------------------------------- PRE
-    if constexpr (CLS == C_EPI || CLS == C_EN) {
+    if constexpr (K == C_EPI || K == C_EN) {
         if (a.pre != PRE_NONE && valid) {
             const R s2 = (R)dyn->s2;
             to_cells();
@@ -539,12 +557,12 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                 int ix, iy, iz;
                 decode(idx, ix, iy, iz);
                 C2<R> v = own(q);
-                if (CLS == C_EPI && a.pre == PRE_VSTEP1) {
+                if (K == C_EPI && a.pre == PRE_VSTEP1) {
                     const R rho = density(a.ph, v);
                     const R V = vext_at(a, idx, ix, iy, iz, it) + dEDFdn(a.ph, rho);
                     a.V[idx] = V;
                     v = cmul(v, phase(a.ph, V));
-                } else if (CLS == C_EPI && a.pre == PRE_PART2) {
+                } else if (K == C_EPI && a.pre == PRE_PART2) {
                     C2<R> p2 = a.psi2[idx];
                     if (a.flags & F_SCALE_PSI2) p2 = cscale(p2, s2);
                     const R rho = density(a.ph, p2);
@@ -555,7 +573,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                     if (a.flags & F_AUX_CPLX) reinterpret_cast<C2<R>*>(a.aux)[idx] = e;
                     else reinterpret_cast<R*>(a.aux)[idx] = lv;
                     v = cmul(v, e);
-                } else if (CLS == C_EN && a.pre == PRE_ENERGY) {
+                } else if (K == C_EN && a.pre == PRE_ENERGY) {
                     const double px = (double)v.x, py = (double)v.y;
                     const double rho = (double)a.ph.gamma * (px * px + py * py);
                     Phys<double> phd;
@@ -570,7 +588,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     }
 
     // ------------------------------------------ dipolar convolution (C_DIP)
-    if constexpr (CLS == C_DIP) {
+    if constexpr (K == C_DIP) {
         const int dm = a.mid;
         if (dm == DIP_DENS_FWD) {
 #pragma unroll
@@ -630,7 +648,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     }
 
     // ------------------------------------------------- energy: forward only
-    if constexpr (CLS == C_EN) {
+    if constexpr (K == C_EN) {
         fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
 #pragma unroll
         for (int q = 0; q < E; q++) {
@@ -640,7 +658,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     }
 
     // -------------------------------------------------- Laplacian pair + MID
-    if constexpr (CLS == C_LAP) {
+    if constexpr (K == C_LAP) {
         if (ops & OP_COPY) {
 #pragma unroll
             for (int q = 0; q < E; q++) slotB[q * NT + tid] = x[q];
@@ -658,7 +676,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
             } else if (a.mid == MID_LAP_ACC) {
 #pragma unroll
                 for (int q = 0; q < E; q++) {
-                    C2<R> l = slotA[q * NT + tid];
+                    C2<R> l = op_lap(q, at(q));
                     if (scale_in) l = cscale(l, s_prev);  // stored from the unscaled psi
                     a.lap[at(q)] = cadd(l, x[q]);
                 }
@@ -669,8 +687,8 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                     const uint32_t idx = at(q);
                     int ix, iy, iz;
                     decode(idx, ix, iy, iz);
-                    const C2<R> L = cadd(slotA[q * NT + tid], own(q));
-                    const C2<R> p = slotB[q * NT + tid];
+                    const C2<R> L = cadd(op_lap(q, idx), own(q));
+                    const C2<R> p = op_copy(q, idx);
                     const R rho = density(a.ph, p);
                     // (qf/Gamma) Im(conj(psi) L) / (rho + eps), L = -lap psi   (dev/gpe_engine.cu:893-918)
                     R vqf = (a.ph.qf_g * (p.x * L.y + (-p.y) * L.x)) / (rho + a.ph.qf_eps);
@@ -700,8 +718,8 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     }
 
     // ---------------------------------------------------------- kinetic pair
-    if constexpr (CLS != C_EN && CLS != C_DIP) {  // the dipolar passes run their own transforms
-        if (CLS != C_LAP || (a.flags & F_KIN)) {
+    if constexpr (K != C_EN && K != C_DIP) {  // the dipolar passes run their own transforms
+        if (K != C_LAP || (a.flags & F_KIN)) {
             fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
 #pragma unroll
             for (int q = 0; q < E; q++) x[q] = cmul(x[q], skt[t + T * q]);
@@ -710,7 +728,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     }
 
     // ------------------------------------------- POST, partial sums, store
-    if constexpr (CLS == C_EPI) {
+    if constexpr (K == C_EPI) {
         if (a.post != POST_NONE && valid) {
             cp_async_wait_all();
             to_cells();
@@ -721,20 +739,20 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                 if (a.post == POST_VSTEP2 || a.post == POST_PART12) {
                     int ix, iy, iz;
                     decode(idx, ix, iy, iz);
-                    R lv = slotC[q * NT + tid];
+                    R lv = op_v(q, idx);
                     const C2<R> pp = cmul(v, phase(a.ph, lv));
                     const R rho = density(a.ph, pp);
                     lv = (lv + vext_at(a, idx, ix, iy, iz, it + 1)) + dEDFdn(a.ph, rho);
-                    if (a.post == POST_PART12 && (a.flags & F_QF)) lv += slotD[q * NT + tid];
+                    if (a.post == POST_PART12 && (a.flags & F_QF)) lv += op_vqf(q, idx);
                     lv = (R)0.5 * lv;
                     const C2<R> e = phase(a.ph, lv);
                     if (a.flags & F_AUX_CPLX) reinterpret_cast<C2<R>*>(a.aux)[idx] = e;
                     else reinterpret_cast<R*>(a.aux)[idx] = lv;
-                    C2<R> p = slotA[q * NT + tid];
+                    C2<R> p = op_psi(q, idx);
                     if (scale_in) p = cscale(p, s_prev);
                     v = cmul(p, e);
                 } else if (a.post == POST_PART1) {
-                    v = cmul(v, phase(a.ph, slotC[q * NT + tid]));
+                    v = cmul(v, phase(a.ph, op_v(q, idx)));
                 } else if (a.post == POST_VSTEP3) {
                     C2<R> e;
                     if (a.flags & F_AUX_CPLX) e = slotA[q * NT + tid];
@@ -756,13 +774,13 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
             }
         }
     }
-    if constexpr (CLS != C_EN) {
+    if constexpr (K != C_EN) {
         if ((a.flags & F_STORE) && valid) {
 #pragma unroll
             for (int q = 0; q < E; q++) a.out[at(q)] = x[q];
         }
     }
-    if constexpr (CLS == C_EPI) {
+    if constexpr (K == C_EPI) {
         if (a.flags & F_LAP_OUT) {
             if (a.flags & F_WZ) {
 #pragma unroll
@@ -784,10 +802,10 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     if constexpr (FIN) {
         if (a.flags & (F_FIN_S2 | F_FIN_STEP | F_FIN_RED)) {
             // energy: 3 sums; norm: 1; a real-time step only advances the step counter
-            constexpr int NR = (CLS == C_EN) ? 3 : 1;
-            const bool sums = (CLS == C_EN) || (a.flags & (F_REDUCE | F_FIN_RED));
+            constexpr int NR = (K == C_EN) ? 3 : 1;
+            const bool sums = (K == C_EN) || (a.flags & (F_REDUCE | F_FIN_RED));
             if (sums) {
-                if constexpr ((CLS == C_EPI || CLS == C_DIP) && sizeof(R) == 4) {
+                if constexpr ((K == C_EPI || K == C_DIP) && sizeof(R) == 4) {
                     if (a.flags & F_REDUCE) acc[0] = block_sum_ff<NT>(nff, sred);
                     else block_sum<NT, NR>(acc, sred);
                 } else {
