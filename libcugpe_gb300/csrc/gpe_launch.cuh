@@ -40,8 +40,17 @@ cudaError_t launch_one(const PassArgs<R>& a, size_t pencils, cudaStream_t st) {
     if (smem > Geo::SMEM_MAX) return cudaErrorInvalidConfiguration;  // more staged operands than a CTA holds
     PassArgs<R> b = a;
     b.npencils = (uint32_t)pencils;
-    pass_kernel<R, N, AX, NT, CLS><<<grid, NT, smem, st>>>(b);
-    return cudaGetLastError();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(NT);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, pass_kernel<R, N, AX, NT, CLS>, b);
 }
 
 template <typename R, int N, int AX>
