@@ -341,6 +341,10 @@ def run_batch_workload(args):
         b.engines[i].set_user_params(c["params"])
         b.engines[i].set_psi(0.0, c["psi"])
     dx2 = np.array([c["dx"] ** 2 for c in ens])
+    # launch configuration of the batched passes chosen by the autotuner (state restored afterwards)
+    t_tune = time.perf_counter()
+    tuned = b.autotune(16)
+    t_tune = time.perf_counter() - t_tune
     done = np.zeros(len(ens), dtype=bool)
     steps = np.zeros(len(ens), dtype=int)
     mu_final = np.full(len(ens), np.nan)
@@ -414,6 +418,7 @@ def run_batch_workload(args):
                             "how": f"FP64 engine, one condensate at a time, first {subset} of each size timed; "
                                    "the others take the mean of their size"},
             "speedup_vs_serial_fp64": t_serial / t_batch,
+            "autotune": dict(tuned, seconds=t_tune, note="not in batch_seconds"),
             "fp32_steps_to_converge": {str(n): [int(x) for x in np.percentile(steps[[j for j, c in enumerate(ens)
                                                   if c["shape"][0] == n and done[j]]], [50, 90, 100])]
                                        if any(done[j] for j, c in enumerate(ens) if c["shape"][0] == n) else None

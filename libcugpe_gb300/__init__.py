@@ -49,7 +49,7 @@ C_ABI_SYMBOLS = [
     "gpe_gb_batch_kernel_launches", "gpe_gb_chemical_potential", "gpe_gb_control_create", "gpe_gb_control_loss",
     "gpe_gb_control_loss_grad", "gpe_gb_control_destroy", "gpe_gb_snapshots_open", "gpe_gb_snapshots_push",
     "gpe_gb_snapshots_close", "gpe_gb_dftc_write_info", "gpe_gb_dftc_read_info", "gpe_gb_set_weizsacker",
-    "gpe_gb_evolve_dipolar", "gpe_gb_energy_dipolar",
+    "gpe_gb_evolve_dipolar", "gpe_gb_energy_dipolar", "gpe_gb_autotune", "gpe_gb_batch_autotune",
 ]
 
 
@@ -82,6 +82,8 @@ def _lib():
             "gpe_gb_set_quantum_friction_coeff": (i, [vp, d]),
             "gpe_gb_set_weizsacker": (i, [vp, d, d]),
             "gpe_gb_evolve_dipolar": (i, [vp, i, dp]),
+            "gpe_gb_autotune": (i, [vp, i, ip, ip, dp]),
+            "gpe_gb_batch_autotune": (i, [vp, i, ip, ip, dp]),
             "gpe_gb_energy_dipolar": (i, [vp, dp, dp]),
             "gpe_gb_set_psi": (i, [vp, d, dp]),
             "gpe_gb_get_psi": (i, [vp, dp, dp]),
@@ -251,6 +253,14 @@ class Engine:
         _check(_lib().gpe_gb_evolve_qf(self._h, int(nt), ctypes.byref(mu)), "evolve_qf")
         return mu.value
 
+    def autotune(self, nsteps=32):
+        """Times each launch configuration on this engine's state and keeps the fastest; psi, time
+        and step counter are restored.  Returns {"direct", "graph_steps", "ms_per_step"}."""
+        d, c, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        _check(_lib().gpe_gb_autotune(self._h, int(nsteps), ctypes.byref(d), ctypes.byref(c), ctypes.byref(ms)),
+               "autotune")
+        return {"direct": d.value, "graph_steps": c.value, "ms_per_step": ms.value}
+
     def evolve_dipolar(self, nt):
         """gpe_evolve_dipolar: nt steps of the dipolar BEC (interactions -2); mu in ITE."""
         mu = ctypes.c_double(0.0)
@@ -360,6 +370,13 @@ class Batch:
 
     def set_active(self, i, active):
         _check(_lib().gpe_gb_batch_set_active(self._h, int(i), 1 if active else 0), "batch_set_active")
+
+    def autotune(self, nsteps=32):
+        """Item order and graph length of the batched passes, timed on the batch's state (restored)."""
+        o, c, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        _check(_lib().gpe_gb_batch_autotune(self._h, int(nsteps), ctypes.byref(o), ctypes.byref(c),
+                                            ctypes.byref(ms)), "batch_autotune")
+        return {"order": o.value, "graph_steps": c.value, "ms_per_step": ms.value}
 
     def chemical_potentials(self):
         """Per condensate: (mu of the last ITE step, running sum of mu)."""

@@ -29,6 +29,7 @@
 #include <string.h>
 #include <limits.h>
 #include <new>
+#include <algorithm>
 #include <vector>
 
 #include "gpe_launch.cuh"
@@ -227,6 +228,8 @@ struct Engine {
     int vslices = 0, vsteps = 1;
 
     bool use_graph = true;
+    int direct_mode = -1;   // operands read where used: -1 by lattice size, 0 staged, 1 direct (autotuner)
+    int graph_chunk = 16;   // steps per replayed graph (autotuner)
     bool graph_dirty = true;
     unsigned version = 0;  // bumped whenever tables or captured arguments change
     bool lap_valid = false;  // lap holds the z-Laplacian term of the current psi
@@ -501,9 +504,9 @@ static PassArgs<R> desc_args(const Engine* e, const PassDesc& d) {
     // ops' operands where used instead of staging them, so the epilogue passes fit 7 CTAs per SM
     // (measured +6% steps/s at 128^3; at 256^3, HBM-resident, the staged prefetch is 6-12% faster).
     // The Weizsaecker sums and currents keep their slots.
-    if (e->prec == GPE_PRECISION_FP32 && e->n <= ((size_t)1 << 21) && e->n3[d.axis] <= 128 &&
-        !(d.flags & (F_WZ | F_DIP)) && d.mid != MID_CURRENT)
-        a.flags |= F_DIRECT;
+    const bool direct_ok = e->prec == GPE_PRECISION_FP32 && e->n3[d.axis] <= 128 && !(d.flags & (F_WZ | F_DIP)) &&
+                           d.mid != MID_CURRENT;
+    if (direct_ok && (e->direct_mode < 0 ? e->n <= ((size_t)1 << 21) : e->direct_mode == 1)) a.flags |= F_DIRECT;
     a.npencils = (uint32_t)pencils_of(e, d.axis);
     return a;
 }
@@ -657,7 +660,7 @@ static int evolve(Engine* e, int nt, double* mu) {
         if ((e->graph_dirty || !e->gexec) && nt - done >= 1) {
             GPE_RC(run_steps(e, s, 1));
             done += 1;
-            if (nt - done >= 2) GPE_RC(build_graph(e, s, nt - done < kGraphSteps ? nt - done : kGraphSteps));
+            if (nt - done >= 2) GPE_RC(build_graph(e, s, nt - done < e->graph_chunk ? nt - done : e->graph_chunk));
         }
         while (e->gexec && nt - done >= e->gsteps) {
             GPE_CK(cudaGraphLaunch(e->gexec, e->st));
@@ -703,6 +706,39 @@ static std::vector<PassDesc> schedule_dipolar(const Engine* e) {
     s.push_back({AX_X, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
     dipolar_half(s, 0u, F_FIN_STEP | (ite ? F_REDUCE : 0u));
     return s;
+}
+
+// State of an engine saved around autotuning runs: psi, the device scalars, the step counter.
+struct Snap {
+    void* psi = nullptr;
+    DynState d;
+    unsigned it = 0;
+    double t0 = 0.0;
+};
+
+static int snap_save(Engine* e, Snap* s) {
+    GPE_CK(cudaMalloc(&s->psi, e->csize() * e->n));
+    GPE_CK(cudaMemcpyAsync(s->psi, e->psi, e->csize() * e->n, cudaMemcpyDeviceToDevice, e->st));
+    GPE_CK(cudaMemcpyAsync(&s->d, e->dyn, sizeof(DynState), cudaMemcpyDeviceToHost, e->st));
+    GPE_CK(cudaStreamSynchronize(e->st));
+    s->it = e->it;
+    s->t0 = e->t0;
+    return 0;
+}
+
+static int snap_load(Engine* e, const Snap* s) {
+    GPE_CK(cudaMemcpyAsync(e->psi, s->psi, e->csize() * e->n, cudaMemcpyDeviceToDevice, e->st));
+    GPE_CK(cudaMemcpyAsync(e->dyn, &s->d, sizeof(DynState), cudaMemcpyHostToDevice, e->st));
+    GPE_CK(cudaStreamSynchronize(e->st));
+    e->it = s->it;
+    e->t0 = s->t0;
+    e->lap_valid = false;
+    return 0;
+}
+
+static void snap_free(Snap* s) {
+    if (s->psi) cudaFree(s->psi);
+    s->psi = nullptr;
 }
 
 static int evolve_dipolar(Engine* e, int nt, double* mu) {
@@ -1222,6 +1258,8 @@ struct gpe_gb_batch {
     cudaGraphExec_t gexec = nullptr;
     int gsteps = 0;
     long long launches = 0;
+    int order = 0;    // item order in a launch: 0 as created, 1 most CTAs first (autotuner)
+    int chunk = 16;   // steps per replayed graph (autotuner)
 };
 
 namespace gpe {
@@ -1265,11 +1303,17 @@ static int batch_build(gpe_gb_batch* b) {
                           : (d.axis == AX_Y) ? batch_shape_axis<AX_Y>(it.n, it.a.npencils, ops, &nctas, &sm)
                                              : batch_shape_axis<AX_Z>(it.n, it.a.npencils, ops, &nctas, &sm);
             if (!ok) return GPE_ERR_LATTICE;
-            it.cta_begin = cta;
             it.nctas = nctas;
-            cta += nctas;
             if (sm > smem) smem = sm;
             items.push_back(it);
+        }
+        // the CTAs of the items with most work first shortens the launch's tail
+        if (b->order == 1)
+            std::stable_sort(items.begin(), items.end(),
+                             [](const BatchItem<float>& x, const BatchItem<float>& y) { return x.nctas > y.nctas; });
+        for (auto& it : items) {
+            it.cta_begin = cta;
+            cta += it.nctas;
         }
         gpe_gb_batch::Launch l;
         l.nitems = (int)items.size();
@@ -1311,7 +1355,7 @@ static int batch_evolve(gpe_gb_batch* b, int nt) {
     // one direct step first (configures the kernels outside capture), then graph replays
     GPE_RC(batch_steps(b, 1));
     done = 1;
-    const int chunk = 16;
+    const int chunk = b->chunk;
     if (nt - done >= chunk && b->gsteps != chunk) {
         cudaGraph_t g = nullptr;
         GPE_CK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
@@ -1934,6 +1978,102 @@ int gpe_gb_control_destroy(gpe_gb_control* hc) {
     gpe::ctl_release(&hc->c);
     delete hc;
     return gpe::cuda_rc(cudaGetLastError());
+}
+
+int gpe_gb_autotune(gpe_gb_engine* h, int nsteps, int* direct, int* chunk, double* ms_per_step) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    Engine* e = &h->e;
+    if (nsteps < 4) nsteps = 4;
+    gpe::Snap snap;
+    GPE_RC(gpe::snap_save(e, &snap));
+    const bool small_axis = e->n3[0] <= 128 || e->n3[1] <= 128 || e->n3[2] <= 128;
+    const int nd = (e->prec == GPE_PRECISION_FP32 && small_axis) ? 2 : 1;
+    const int chunks[3] = {8, 16, 32};
+    double best = 1e300;
+    int bd = 0, bc = 16, rc = 0;
+    cudaEvent_t a = nullptr, b = nullptr;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    for (int d = 0; d < nd && !rc; d++) {
+        for (int c = 0; c < 3 && !rc; c++) {
+            e->direct_mode = d;
+            e->graph_chunk = chunks[c];
+            gpe::drop_graph(e);
+            e->graph_dirty = true;
+            if ((rc = gpe::snap_load(e, &snap))) break;
+            if ((rc = gpe::evolve(e, nsteps, nullptr))) break;  // builds the graph
+            if ((rc = gpe::snap_load(e, &snap))) break;
+            cudaEventRecord(a, e->st);
+            if ((rc = gpe::evolve(e, nsteps, nullptr))) break;
+            cudaEventRecord(b, e->st);
+            cudaEventSynchronize(b);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, a, b);
+            if (ms < best) { best = ms; bd = d; bc = chunks[c]; }
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    e->direct_mode = (nd == 2) ? bd : -1;
+    e->graph_chunk = bc;
+    gpe::drop_graph(e);
+    e->graph_dirty = true;
+    const int rc2 = gpe::snap_load(e, &snap);
+    gpe::snap_free(&snap);
+    if (rc) return rc;
+    if (rc2) return rc2;
+    if (direct) *direct = e->direct_mode;
+    if (chunk) *chunk = e->graph_chunk;
+    if (ms_per_step) *ms_per_step = best / nsteps;
+    return 0;
+}
+
+int gpe_gb_batch_autotune(gpe_gb_batch* bt, int nsteps, int* order, int* chunk, double* ms_per_step) {
+    if (!bt) return GPE_ERR_ARGUMENT;
+    if (nsteps < 4) nsteps = 4;
+    std::vector<gpe::Snap> snaps(bt->eng.size());
+    int rc = 0;
+    for (size_t i = 0; i < bt->eng.size() && !rc; i++) rc = gpe::snap_save(&bt->eng[i]->e, &snaps[i]);
+    auto restore = [&]() -> int {
+        for (size_t i = 0; i < bt->eng.size(); i++) GPE_RC(gpe::snap_load(&bt->eng[i]->e, &snaps[i]));
+        return 0;
+    };
+    const int chunks[3] = {8, 16, 32};
+    double best = 1e300;
+    int bo = 0, bc = 16;
+    cudaEvent_t a = nullptr, b = nullptr;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    for (int o = 0; o < 2 && !rc; o++) {
+        for (int c = 0; c < 3 && !rc; c++) {
+            bt->order = o;
+            bt->chunk = chunks[c];
+            bt->dirty = true;
+            if ((rc = restore())) break;
+            if ((rc = gpe::batch_evolve(bt, nsteps))) break;  // builds items and graph
+            if ((rc = restore())) break;
+            cudaEventRecord(a, bt->st);
+            if ((rc = gpe::batch_evolve(bt, nsteps))) break;
+            cudaEventRecord(b, bt->st);
+            cudaEventSynchronize(b);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, a, b);
+            if (ms < best) { best = ms; bo = o; bc = chunks[c]; }
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    bt->order = bo;
+    bt->chunk = bc;
+    bt->dirty = true;
+    const int rc2 = rc ? 0 : restore();
+    for (auto& s : snaps) gpe::snap_free(&s);
+    if (rc) return rc;
+    if (rc2) return rc2;
+    if (order) *order = bo;
+    if (chunk) *chunk = bc;
+    if (ms_per_step) *ms_per_step = best / nsteps;
+    return 0;
 }
 
 const char* gpe_gb_error_string(int code) {

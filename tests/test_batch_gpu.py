@@ -69,3 +69,20 @@ def test_batch_rejects_unsupported(cuda_device, gpe_lib):
         g.Batch([(16, 16, 16)], precision=g.FP32)
     with pytest.raises(g.GPEError):
         g.Batch([(32, 32, 32)], precision=g.FP64)
+
+
+def test_batch_autotune_keeps_results(cuda_device, gpe_lib):
+    """Item order and graph length change neither the state (restored) nor the bits of later steps."""
+    def make():
+        b = g.Batch(SHAPES, interactions=-1, alpha=0.0, beta=1.0, dt=0.05, npart=[1.0] * len(SHAPES))
+        for i, s in enumerate(SHAPES):
+            b.engines[i].set_user_params(params_for(i))
+            b.engines[i].set_psi(0.0, configs.random_state(s, seed=50 + i))
+        return b
+    b1, b2 = make(), make()
+    choice = b1.autotune(8)
+    assert choice["order"] in (0, 1) and choice["graph_steps"] in (8, 16, 32)
+    b1.evolve(21)
+    b2.evolve(21)
+    for i in range(len(SHAPES)):
+        assert np.array_equal(b1.engines[i].get_psi()[1], b2.engines[i].get_psi()[1]), i

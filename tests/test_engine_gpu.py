@@ -343,3 +343,23 @@ def test_dipolar_fp32_against_fp64_oracle(cuda_device, gpe_lib):
     o.evolve_dipolar(20)
     assert rel(e.get_psi()[1], o.get_psi()[1]) <= 20 * TOL_FP32_STEP
     assert e.energy_dipolar()[1] == pytest.approx(o.energy_dipolar(), rel=1e-5)
+
+
+@pytest.mark.parametrize("precision", [g.FP32, g.FP64])
+def test_autotune_restores_state_and_keeps_results(cuda_device, gpe_lib, precision):
+    """The autotuner runs the engine's own state under each configuration, puts it back, and every
+    configuration it may pick computes the same bits."""
+    shape = (32, 16, 64)
+    e, _, psi = make_pair(shape, "ufg_rte_qf", precision=precision)
+    ref, _, _ = make_pair(shape, "ufg_rte_qf", precision=precision)
+    e.evolve_qf(3)
+    ref.evolve_qf(3)
+    before = e.get_psi()
+    choice = e.autotune(8)
+    assert choice["graph_steps"] in (8, 16, 32) and choice["ms_per_step"] > 0
+    assert choice["direct"] in ((0, 1) if precision == g.FP32 else (-1,))
+    after = e.get_psi()
+    assert after[0] == before[0] and np.array_equal(after[1], before[1])
+    e.evolve_qf(20)
+    ref.evolve_qf(20)
+    assert np.array_equal(e.get_psi()[1], ref.get_psi()[1])
