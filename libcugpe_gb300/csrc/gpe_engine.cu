@@ -814,6 +814,40 @@ static int evolve_enforced(Engine* e, int nt, double* mu, int mode) {
     return cuda_rc(cudaGetLastError());
 }
 
+// E_W = (lambda/8) sum |grad rho|^2 / (rho + eps) from the gradient sums wg -> d->red[slot];
+// fixed grid, deterministic order
+template <typename R>
+__global__ void __launch_bounds__(kRedThreads) k_wz_energy(const C2<R>* psi, const R* wg, size_t n, double gamma,
+                                                           double lam8, double eps, double* partials, DynState* d,
+                                                           int slot) {
+    __shared__ double sw[kRedThreads / 32];
+    __shared__ bool last;
+    double acc = 0.0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double x = psi[i].x, y = psi[i].y;
+        acc += (double)wg[i] / (gamma * (x * x + y * y) + eps);
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < kRedThreads / 32; w++) s += sw[w];
+        partials[blockIdx.x] = s;
+        __threadfence();
+        last = (atomicAdd(&d->ticket, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        double s = 0.0;
+        for (unsigned b = 0; b < gridDim.x; b++) s += __ldcg(partials + b);
+        d->red[slot] = lam8 * s;
+        d->ticket = 0;
+        __threadfence();
+    }
+}
+
 template <typename R>
 static int norm_to_slot(Engine* e, int slot) {
     k_norm<R><<<kRedBlocks, kRedThreads, 0, e->st>>>((const C2<R>*)e->psi, e->n, e->gamma, e->partials, e->dyn, slot);
@@ -851,11 +885,25 @@ static int energy(Engine* e, double* ekin, double* eint, double* eext) {
         e->launches++;
         GPE_RC(cuda_rc(launch_pass<R>(a, e->n3[axis], axis, pencils_of(e, axis), e->st)));
     }
+    double ew = 0.0;
+    if (e->wz != 0.0) {
+        // Weizsaecker energy: the gradient sums of the three Laplacian passes, then one reduction
+        const PassDesc wz[3] = {{AX_Z, PRE_NONE, MID_LAP_STORE, POST_NONE, F_LAP | F_WZ, B_PSI, B_NONE},
+                                {AX_Y, PRE_NONE, MID_LAP_ACC, POST_NONE, F_LAP | F_WZ, B_PSI, B_NONE},
+                                {AX_X, PRE_NONE, MID_LAP_ACC, POST_NONE, F_LAP | F_WZ, B_PSI, B_NONE}};
+        for (const PassDesc& d : wz) GPE_RC(launch_desc<R>(e, d));
+        e->lap_valid = false;
+        k_wz_energy<R><<<kRedBlocks, kRedThreads, 0, e->st>>>((const C2<R>*)e->psi, (const R*)e->wg, e->n, e->gamma,
+                                                               e->wz / 8.0, e->wz_eps, e->partials, e->dyn, 10);
+        e->launches++;
+        GPE_CK(cudaGetLastError());
+        GPE_CK(cudaMemcpyAsync(&ew, &e->dyn->red[10], sizeof ew, cudaMemcpyDeviceToHost, e->st));
+    }
     double red[9];
     GPE_CK(cudaMemcpyAsync(red, e->dyn->red, sizeof red, cudaMemcpyDeviceToHost, e->st));
     GPE_CK(cudaStreamSynchronize(e->st));
     *eext = red[0];
-    *eint = red[1];
+    *eint = red[1] + ew;
     *ekin = (red[2] + red[5]) + red[8];
     return 0;
 }

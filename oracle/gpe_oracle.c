@@ -434,7 +434,35 @@ static void qf_potential(gpe_oracle *o, const cd *psi) {
  * lap rho = 2 Gamma (Re(conj(psi) lap psi) + |grad psi|^2),
  * derivatives of psi spectral on the reference k grid (dev/gpe_engine.cu:147-154),
  * rho replaced by rho + wz_eps in both denominators. */
+static void wz_sums(gpe_oracle *o, const cd *psi);
+
 static void wz_potential(gpe_oracle *o, const cd *psi) {
+    const long n = (long)o->n;
+    const double g2 = 2.0 * o->gamma;
+    wz_sums(o, psi);
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+    for (long i = 0; i < n; i++) {
+        const cd p = psi[i], l = o->wz1[i];
+        const double inv = 1.0 / (density(o, p) + o->wz_eps);
+        const double lrho = g2 * ((p.x * l.x + p.y * l.y) + o->wzS[i]);
+        o->Vqf[i] += (o->wz / 8.0) * (o->wzG[i] * inv * inv - 2.0 * lrho * inv);
+    }
+}
+
+/* E_W = (lambda/8) sum |grad rho|^2 / (rho + eps) */
+static double wz_energy(gpe_oracle *o, const cd *psi) {
+    const long n = (long)o->n;
+    wz_sums(o, psi);
+    double *w = (double *)malloc(sizeof(double) * n);
+#pragma omp parallel for num_threads(o->nthreads) schedule(static)
+    for (long i = 0; i < n; i++) w[i] = o->wzG[i] / (density(o, psi[i]) + o->wz_eps);
+    const double e = (o->wz / 8.0) * det_sum(o, w);
+    free(w);
+    return e;
+}
+
+/* wzG = sum_a (d_a rho)^2, wzS = sum_a |d_a psi|^2, wz1 = lap psi */
+static void wz_sums(gpe_oracle *o, const cd *psi) {
     const int ny = o->ny, nz = o->nz;
     const long n = (long)o->n;
     const double inv_n = 1.0 / (double)o->n, g2 = 2.0 * o->gamma;
@@ -467,13 +495,6 @@ static void wz_potential(gpe_oracle *o, const cd *psi) {
         o->wz1[i] = cscale(o->wrk3C[i], -k2 * inv_n);
     }
     fft3d(o, o->wz1, +1);
-#pragma omp parallel for num_threads(o->nthreads) schedule(static)
-    for (long i = 0; i < n; i++) {
-        const cd p = psi[i], l = o->wz1[i];
-        const double inv = 1.0 / (density(o, p) + o->wz_eps);
-        const double lrho = g2 * ((p.x * l.x + p.y * l.y) + o->wzS[i]);
-        o->Vqf[i] += (o->wz / 8.0) * (o->wzG[i] * inv * inv - 2.0 * lrho * inv);
-    }
 }
 
 /* potential frozen over a step: friction (dev/gpe_engine.cu:893-933) and the Weizsaecker term */
@@ -641,6 +662,7 @@ int oracle_energy(void *h, double *t, double *ekin, double *eint, double *eext) 
     }
     *eext = det_sum(o, w1);
     *eint = det_sum(o, w2);
+    if (o->wz != 0.0) *eint += wz_energy(o, o->psi);  /* Weizsaecker term (not in the reference) */
     memcpy(o->psi2, o->psi, sizeof(cd) * o->n);
     fft3d(o, o->psi2, -1);
     const double den = 2.0 * o->gamma * (double)o->n;

@@ -363,3 +363,15 @@ def test_autotune_restores_state_and_keeps_results(cuda_device, gpe_lib, precisi
     e.evolve_qf(20)
     ref.evolve_qf(20)
     assert np.array_equal(e.get_psi()[1], ref.get_psi()[1])
+
+
+@pytest.mark.parametrize("precision", [g.FP64, g.FP32])
+def test_weizsacker_energy_matches_oracle(cuda_device, gpe_lib, precision):
+    """energy() includes E_W = (lambda/8) sum |grad rho|^2/(rho + eps) in eint."""
+    shape = (32, 16, 16)
+    e, o, _ = make_wz_pair(shape, "ufg_ite_qf", precision=precision)
+    e.evolve_qf(2)
+    o.evolve_qf(2)
+    tol = 1e-10 if precision == g.FP64 else 2e-5
+    for a, b in zip(e.energy()[1:], o.energy()[1:]):
+        assert abs(a - b) <= tol * max(1.0, abs(b)), (a, b)

@@ -253,3 +253,21 @@ def test_oracle_dipolar_potential_and_energy():
     o.change_alpha_beta(0.0, 1.0)
     mu = o.evolve_dipolar(3)
     assert np.isfinite(mu) and o.get_norm() == pytest.approx(1.0, rel=1e-13)
+
+
+def test_oracle_weizsacker_energy_gaussian():
+    """E_W = (lambda/8) sum |grad rho|^2/rho = (lambda/8) N sum_a 1/s_a^2 for a Gaussian density of
+    variances s_a^2; energy() adds it to the interaction energy."""
+    shape, s, lam = (64, 32, 32), (3.0, 2.0, 2.0), 0.25
+    X, Y, Z = [np.arange(n, dtype=float)[tuple(slice(None) if b == a else None for b in range(3))] - n // 2
+               for a, n in enumerate(shape)]
+    psi = (np.exp(-X ** 2 / (4 * s[0] ** 2) - Y ** 2 / (4 * s[1] ** 2) - Z ** 2 / (4 * s[2] ** 2)) *
+           np.ones(shape)).astype(np.complex128)
+    o = oracle.Oracle(shape, 0, 0.0, 1.0, 0.05, 1.0, threads=4)
+    o.set_user_params([0.04, 0.04, 0.04, 0.0])
+    o.set_psi(0.0, psi)
+    _, _, eint0, _ = o.energy()
+    o.set_weizsacker(lam, 1e-14)
+    _, _, eint1, _ = o.energy()
+    N = np.sum(2.0 * np.abs(psi) ** 2)
+    assert eint1 - eint0 == pytest.approx(lam / 8 * N * sum(1 / x ** 2 for x in s), rel=1e-9)
