@@ -386,7 +386,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     __shared__ double sred[FIN ? NT / 32 : 1][NRED];
     __shared__ bool last_cta;
 
-    // Programmatic dependent launch: the pass kernels are launched so that their CTAs may start
+    // Programmatic dependent launch: the FP32 pass kernels are launched so that their CTAs may start
     // while the previous pass drains; every global read below comes after the wait for that pass
     // to complete (a no-op for a launch without the attribute).  Dependents may be launched as
     // soon as every CTA of this pass is running.
