@@ -35,8 +35,23 @@ cudaError_t launch_one(const PassArgs<R>& a, size_t pencils, cudaStream_t st) {
         if (e != cudaSuccess) return e;
         configured = true;
     }
-    const unsigned grid = (unsigned)((pencils + Geo::W - 1) / Geo::W);
-    const size_t smem = Geo::SMEM_BASE + slot_bytes<R>(staged_ops(a.mid, a.post, a.flags), Geo::E * NT);
+    unsigned grid = (unsigned)((pencils + Geo::W - 1) / Geo::W);
+    size_t smem = Geo::SMEM_BASE + slot_bytes<R>(staged_ops(a.mid, a.post, a.flags), Geo::E * NT);
+    if constexpr (CLS == C_KINP) {
+        // persistent: one staging buffer per CTA, as many CTAs as fit on the GPU at once
+        smem = Geo::SMEM_BASE + (size_t)Geo::E * NT * sizeof(C2<R>);
+        static unsigned resident = 0;  // per instantiation, single device
+        if (!resident) {
+            int per_sm = 0, sms = 0, dev = 0;
+            cudaError_t e = cudaGetDevice(&dev);
+            if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (e == cudaSuccess)
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pass_kernel<R, N, AX, NT, CLS>, NT, smem);
+            if (e != cudaSuccess) return e;
+            resident = (unsigned)((per_sm > 0 ? per_sm : 1) * sms);
+        }
+        if (grid > resident) grid = resident;
+    }
     if (smem > Geo::SMEM_MAX) return cudaErrorInvalidConfiguration;  // more staged operands than a CTA holds
     PassArgs<R> b = a;
     b.npencils = (uint32_t)pencils;
@@ -60,7 +75,14 @@ cudaError_t launch_ax(const PassArgs<R>& a, size_t pencils, cudaStream_t st, uns
     constexpr int NT = pass_nt<R, N, AX>();
     *grid_out = (unsigned)((pencils + PassGeom<R, N, AX, NT>::W - 1) / PassGeom<R, N, AX, NT>::W);
     switch (op_class(a.pre, a.mid, a.post, a.flags)) {
-        case C_KIN: return launch_one<R, N, AX, NT, C_KIN>(a, pencils, st);
+        case C_KIN:
+            // long FP32 pencils (HBM-resident lattices): the persistent pass overlaps loads and transforms
+            if constexpr (sizeof(R) == 4 && N >= 256) {
+                if ((a.flags & ~(F_VEXTRA | F_DIRECT)) == (F_KIN | F_STORE) && a.pre == PRE_NONE &&
+                    a.mid == MID_NONE && a.post == POST_NONE)
+                    return launch_one<R, N, AX, NT, C_KINP>(a, pencils, st);
+            }
+            return launch_one<R, N, AX, NT, C_KIN>(a, pencils, st);
         case C_EPI: return launch_one<R, N, AX, NT, C_EPI>(a, pencils, st);
         case C_LAP: return launch_one<R, N, AX, NT, C_LAP>(a, pencils, st);
         case C_DIP: return launch_one<R, N, AX, NT, C_DIP>(a, pencils, st);

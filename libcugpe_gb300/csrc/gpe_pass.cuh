@@ -353,7 +353,8 @@ struct PassGeom {
 
 // Kernel classes: each instantiation compiles only the code its passes use,
 // which keeps register use and instruction footprint down.
-enum : int { C_KIN = 0, C_EPI = 1, C_LAP = 2, C_EN = 3, C_DIP = 4, C_EPI_D = 5, C_LAP_D = 6 };
+enum : int { C_KIN = 0, C_EPI = 1, C_LAP = 2, C_EN = 3, C_DIP = 4, C_EPI_D = 5, C_LAP_D = 6, C_KINP = 7 };
+// C_KINP: persistent kinetic pass (kin_pipe_body) chosen by the launcher for long FP32 pencils.
 // C_EPI_D / C_LAP_D: the epilogue and Laplacian classes reading their operands where used (F_DIRECT),
 // compiled separately so the staged variants keep their register allocation.
 
@@ -835,10 +836,91 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     }
 }
 
+// Persistent kinetic pass (FFT_a, x kinetic factor, inverse FFT_a) for HBM-resident lattices: each CTA
+// walks tiles of W pencils grid-stride, and while it transforms one tile the next tile's points are
+// already on their way into shared memory (cp.async into a staging buffer that only the copying
+// thread reads back), so the loads of one tile overlap the arithmetic of the previous one.
+template <typename R, int N, int AX, int NT>
+__device__ __forceinline__ void kin_pipe_body(const PassArgs<R>& a) {
+    using Geo = PassGeom<R, N, AX, NT>;
+    constexpr int E = Geo::E, T = Geo::T, CW = Geo::CW, G = Geo::G, W = Geo::W, ROW = Geo::ROW;
+    constexpr int SSTR = (AX == AX_Z) ? 1 : CW;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    C2<R>* stw = reinterpret_cast<C2<R>*>(smem_raw);
+    C2<R>* skt = stw + Geo::TW;
+    C2<R>* sx = reinterpret_cast<C2<R>*>(smem_raw + Geo::TAB_BYTES);
+    C2<R>* stg = reinterpret_cast<C2<R>*>(smem_raw + Geo::SMEM_BASE);
+    const int tid = threadIdx.x;
+    for (int i = tid; i < Geo::TW; i += NT) stw[i] = a.tw[i];
+    for (int i = tid; i < N; i += NT) skt[i] = a.ktab[i];
+    int pl, t, bar;
+    C2<R>* sb;
+    if constexpr (AX == AX_Z) {
+        const int w = tid >> 5, lane = tid & 31;
+        t = lane % T;
+        pl = w * CW + lane / T;
+        sb = sx + pl * ROW;
+        bar = 0;
+    } else {
+        const int gi = tid / G, loc = tid % G;
+        const int c = loc % CW;
+        t = loc / CW;
+        pl = gi * CW + c;
+        sb = sx + gi * (ROW * CW) + c;
+        bar = 1 + gi;
+    }
+    const int ly = a.ly, lz = a.lz;
+    const uint32_t lstr = (AX == AX_Z) ? 0u : (AX == AX_Y) ? (uint32_t)lz : (uint32_t)(ly + lz);
+    auto tbase = [&](uint32_t tile, bool& valid) -> uint32_t {
+        const uint32_t gp = tile * (uint32_t)W + pl;
+        valid = gp < a.npencils;
+        uint32_t base;
+        if constexpr (AX == AX_Z) base = gp << lz;
+        else if constexpr (AX == AX_Y) base = (((gp >> lz) << ly) << lz) + (gp & ((1u << lz) - 1));
+        else base = gp;
+        return base + ((uint32_t)t << lstr);
+    };
+    const uint32_t ntiles = (a.npencils + W - 1) / W;
+    auto prefetch = [&](uint32_t tile) {
+        bool v;
+        const uint32_t tb = tbase(tile, v);
+        if (v) {
+#pragma unroll
+            for (int q = 0; q < E; q++)
+                cp_async(stg + q * NT + tid, a.in + tb + ((uint32_t)(T * q) << lstr), sizeof(C2<R>));
+        }
+        cp_async_commit();
+    };
+    uint32_t tile = blockIdx.x;
+    if (tile < ntiles) prefetch(tile);
+    __syncthreads();  // tables staged
+    for (; tile < ntiles; tile += gridDim.x) {
+        bool valid;
+        const uint32_t tb = tbase(tile, valid);
+        cp_async_wait_all();
+        C2<R> x[E];
+#pragma unroll
+        for (int q = 0; q < E; q++) x[q] = valid ? stg[q * NT + tid] : mk<R>((R)0, (R)0);
+        if (tile + gridDim.x < ntiles) prefetch(tile + gridDim.x);
+        fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
+#pragma unroll
+        for (int q = 0; q < E; q++) x[q] = cmul(x[q], skt[t + T * q]);
+        fft<R, N, true, SSTR, G>(x, sb, t, stw, bar);
+        if (valid) {
+#pragma unroll
+            for (int q = 0; q < E; q++) a.out[tb + ((uint32_t)(T * q) << lstr)] = x[q];
+        }
+    }
+    cp_async_wait_all();
+}
+
 template <typename R, int N, int AX, int NT, int CLS>
 __global__ void __launch_bounds__(NT, PassGeom<R, N, AX, NT>::MINB)
 pass_kernel(const PassArgs<R> a) {
-    pass_body<R, N, AX, NT, CLS>(a, blockIdx.x, gridDim.x);
+    if constexpr (CLS == C_KINP) kin_pipe_body<R, N, AX, NT>(a);
+    else pass_body<R, N, AX, NT, CLS>(a, blockIdx.x, gridDim.x);
 }
 
 }  // namespace gpe

@@ -375,3 +375,14 @@ def test_weizsacker_energy_matches_oracle(cuda_device, gpe_lib, precision):
     tol = 1e-10 if precision == g.FP64 else 2e-5
     for a, b in zip(e.energy()[1:], o.energy()[1:]):
         assert abs(a - b) <= tol * max(1.0, abs(b)), (a, b)
+
+
+@pytest.mark.parametrize("shape", [(16, 256, 16), (512, 16, 8), (8, 8, 512), (256, 256, 16)])
+def test_fp32_long_pencils_against_oracle(cuda_device, gpe_lib, shape):
+    """FP32 pencils of 256 and 512 points (persistent kinetic passes with prefetch, 256/512-thread CTAs
+    on x) against the FP64 oracle, plain and friction schedules."""
+    for case in ("bec_rte", "ufg_rte_qf"):
+        e, o, _ = make_pair(shape, case, precision=g.FP32)
+        e.evolve_qf(2)
+        o.evolve_qf(2)
+        assert rel(e.get_psi()[1], o.get_psi()[1]) <= 2 * TOL_FP32_STEP, (case, rel(e.get_psi()[1], o.get_psi()[1]))
