@@ -76,8 +76,9 @@ cudaError_t launch_ax(const PassArgs<R>& a, size_t pencils, cudaStream_t st, uns
     *grid_out = (unsigned)((pencils + PassGeom<R, N, AX, NT>::W - 1) / PassGeom<R, N, AX, NT>::W);
     switch (op_class(a.pre, a.mid, a.post, a.flags)) {
         case C_KIN:
-            // long FP32 pencils (HBM-resident lattices): the persistent pass overlaps loads and transforms
-            if constexpr (sizeof(R) == 4 && N >= 256) {
+            // FP32 x pencils of 512 points: the persistent pass overlaps loads and transforms (measured
+            // 923 -> 809 us per pass at 512^3; on y pencils and at 256 points it was slower)
+            if constexpr (sizeof(R) == 4 && N >= 512 && AX == AX_X) {
                 if ((a.flags & ~(F_VEXTRA | F_DIRECT)) == (F_KIN | F_STORE) && a.pre == PRE_NONE &&
                     a.mid == MID_NONE && a.post == POST_NONE)
                     return launch_one<R, N, AX, NT, C_KINP>(a, pencils, st);
