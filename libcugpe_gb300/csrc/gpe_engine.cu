@@ -642,7 +642,6 @@ static int finish_ite(Engine* e) {
     return cuda_rc(cudaGetLastError());
 }
 
-static const int kGraphSteps = 16;
 
 static int evolve(Engine* e, int nt, double* mu) {
     if (nt <= 0) return 0;
