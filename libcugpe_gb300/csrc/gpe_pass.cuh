@@ -4,7 +4,7 @@
 // runs, in order,
 //   load -> PRE op -> [LAP pair: FFT, x k_a^2 table, inverse FFT -> MID op]
 //        -> [KIN pair: FFT, x exp(c k_a^2)/N_a table, inverse FFT] -> POST op
-//        -> store (+ FP64 partial sums, finalised by the last CTA).
+//        -> store (+ partial sums, finalised by the last CTA).
 // The PRE/MID/POST ops are the reference's pointwise kernels
 // (dev/gpe_engine.cu:716-918), fused into the pass that already holds the
 // point in registers; a host-side schedule (gpe_engine.cu) strings the passes
