@@ -1,0 +1,86 @@
+"""A driver written against the reference API (include/gpe_engine.h, C++ linkage, lattice and
+functional fixed with -DNX -DNY -DNZ -DINTERACTIONS as the reference's drivers are built) runs end to
+end on the GPU through libgpe_gb300.so; its psi, mu and energies match the CPU oracle."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+from libcugpe_gb300 import configs
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+DRIVER = r"""
+#include <cstdio>
+#include <vector>
+#include "gpe_engine.h"
+// ITE with normalisation, then RTE with quantum friction, as test_compare/gpe_imag.c and gpe_real.c do
+int main(int argc, char** argv) {
+    int nx, ny, nz;
+    gpe_get_lattice(&nx, &ny, &nz);
+    const size_t n = (size_t)nx * ny * nz;
+    std::vector<cuCplx> psi(n);
+    FILE* f = fopen(argv[1], "rb");
+    if (!f || fread(psi.data(), sizeof(cuCplx), n, f) != n) return 3;
+    fclose(f);
+    double p[4] = {0.04, 0.04, 0.06, 0.0}, mu = 0.0, t, ek, ei, ee;
+    int ierr = 0;
+    gpe_exec(gpe_create_engine(0.0, 1.0, 0.05, 1000.0), ierr);
+    gpe_exec(gpe_set_user_params(4, p), ierr);
+    gpe_exec(gpe_set_psi(0.0, psi.data()), ierr);
+    gpe_exec(gpe_normalize_psi(), ierr);
+    gpe_exec(gpe_evolve_qf(20, &mu), ierr);
+    gpe_exec(gpe_energy(&t, &ek, &ei, &ee), ierr);
+    printf("ITE %.17g %.17g %.17g %.17g %.17g\n", mu, t, ek, ei, ee);
+    gpe_exec(gpe_set_rte_evolution(), ierr);
+    gpe_exec(gpe_set_quantum_friction_coeff(0.1), ierr);
+    gpe_exec(gpe_evolve_qf(15), ierr);
+    gpe_exec(gpe_get_psi(&t, psi.data()), ierr);
+    FILE* g = fopen(argv[2], "wb");
+    fwrite(psi.data(), sizeof(cuCplx), n, g);
+    fclose(g);
+    gpe_exec(gpe_energy(&t, &ek, &ei, &ee), ierr);
+    printf("RTE %.17g %.17g %.17g %.17g\n", t, ek, ei, ee);
+    gpe_exec(gpe_destroy_engine(), ierr);
+    return ierr;
+}
+"""
+
+
+def test_reference_style_driver_runs_on_gpu(cuda_device, gpe_lib, tmp_path):
+    shape = (16, 32, 16)
+    src, exe = tmp_path / "driver.cpp", tmp_path / "driver"
+    src.write_text(DRIVER)
+    cmd = ["g++", "-O2", "-DNX=16", "-DNY=32", "-DNZ=16", "-DINTERACTIONS=0", "-I", os.path.join(ROOT, "include"),
+           "-I", "/usr/local/cuda/include", str(src), "-L", os.path.dirname(gpe_lib), "-lgpe_gb300",
+           "-Wl,-rpath," + os.path.dirname(gpe_lib), "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    psi0 = configs.random_state(shape, seed=41, npart=1000.0, gamma=2.0)
+    inp, outp = tmp_path / "psi0.bin", tmp_path / "psi1.bin"
+    psi0.astype(np.complex128).tofile(inp)
+    r = subprocess.run([str(exe), str(inp), str(outp)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = {l.split()[0]: [float(x) for x in l.split()[1:]] for l in r.stdout.splitlines() if l.strip()}
+    o = oracle.Oracle(shape, 0, 0.0, 1.0, 0.05, 1000.0, threads=4)
+    o.set_user_params([0.04, 0.04, 0.06, 0.0])
+    o.set_psi(0.0, psi0)
+    o.normalize_psi()
+    mu = o.evolve_qf(20)
+    t, ek, ei, ee = o.energy()
+    assert lines["ITE"][0] == pytest.approx(mu, rel=1e-10)
+    for a, b in zip(lines["ITE"][2:], (ek, ei, ee)):
+        assert a == pytest.approx(b, rel=1e-10)
+    o.change_alpha_beta(1.0, 0.0)
+    o.set_quantum_friction_coeff(0.1)
+    o.evolve_qf(15)
+    _, po = o.get_psi()
+    ours = np.fromfile(outp, dtype=np.complex128).reshape(shape)
+    assert float(np.linalg.norm(ours - po) / np.linalg.norm(po)) <= 1e-11
+    t, ek, ei, ee = o.energy()
+    for a, b in zip(lines["RTE"][1:], (ek, ei, ee)):
+        assert a == pytest.approx(b, rel=1e-10)
