@@ -28,31 +28,52 @@ CASES = [
     ("bec_rte_32x16x8", (32, 16, 8), -1, 1.0, 0.0, 0.05, 1.0, [0.0625, 0.05, 0.07, 31.83], 0.0, [1, 9], 2),
     ("ufg_rte_qf_16", (16, 16, 16), 0, 1.0, 0.0, 0.05, 1000.0, [0.04, 0.04, 0.06, 0.0], 0.1, [1, 6], 3),
     ("ufg_ite_qf_8x32x16", (8, 32, 16), 0, 0.0, 1.0, 0.05, 1000.0, [0.04, 0.04, 0.06, 0.0], 0.1, [1, 6], 4),
+    ("becside_ite_16", (16, 16, 16), 1, 0.0, 1.0, 0.05, 100.0, [0.05, 0.05, 0.05, 2.0], 0.0, [1, 6], 5),
+    ("ufg_rte_currents_16x8x32", (16, 8, 32), 0, 1.0, 0.0, 0.05, 1000.0, [0.04, 0.05, 0.06, 0.0], 0.1, [1, 4], 6),
+    # dipolar BEC (gpe_evolve_dipolar), fifth user parameter A_DIP
+    ("dipolar_rte_16x8x32", (16, 8, 32), -2, 1.0, 0.0, 0.05, 1.0, [0.0625, 0.0625, 0.05, 2.0, 1.5], 0.0, [1, 6], 7),
+    ("dipolar_ite_16", (16, 16, 16), -2, 0.0, 1.0, 0.05, 1.0, [0.0625, 0.0625, 0.05, 2.0, 1.5], 0.0, [1, 6], 8),
 ]
 
 
-def main(outdir=HERE):
+def main(outdir=HERE, only=None):
     os.makedirs(outdir, exist_ok=True)
     for name, shape, inter, alpha, beta, dt, npart, params, qf, steps, seed in CASES:
-        gamma = 1.0 if inter == -1 else 2.0
+        if only and name not in only:
+            continue
+        gamma = 1.0 if inter < 0 else 2.0
+        dipolar = inter == -2
+        currents = "currents" in name
         psi0 = configs.random_state(shape, seed=seed, npart=npart, gamma=gamma)
         cmds = (["N"] if beta != 0 else [])
+        if dipolar:
+            cmds += [f"A{params[4]!r}"]
         for s in steps:
-            cmds += [f"S{s}", "D"]
+            cmds += [f"Y{s}" if dipolar else f"S{s}", "D"]
+        if currents:
+            cmds += ["J"]
+        if dipolar:
+            cmds += ["W"]
         cmds += ["E"]
-        out = ref_run.run(shape, inter, alpha, beta, dt, npart, params, psi0, cmds, qf=qf)
+        out = ref_run.run(shape, inter, alpha, beta, dt, npart, params[:4], psi0, cmds, qf=qf)
         arrays = {"psi0": psi0}
         for k, p in enumerate(out["psi"]):
             arrays[f"psi_{k}"] = p
+        if currents:
+            for a, j in zip("xyz", out["currents"][0]):
+                arrays["j" + a] = j
         np.savez_compressed(os.path.join(outdir, name + ".npz"), **arrays)
         meta = {"shape": list(shape), "interactions": inter, "alpha": alpha, "beta": beta, "dt": dt,
                 "npart": npart, "params": params, "qf": qf, "steps": steps, "seed": seed,
                 "normalize_first": beta != 0, "mu": out["mu"], "energy": list(out["energy"][-1][1:]),
+                "evolve": "dipolar" if dipolar else "qf", "currents": currents,
                 "tol_psi": 1e-12, "source": "reference libcugpe dev/ engine built for sm_103a by oracle/build_ref.py"}
+        if dipolar:
+            meta["edip"] = out["edip"][-1]
         with open(os.path.join(outdir, name + ".json"), "w") as fh:
             json.dump(meta, fh, indent=1)
         print(name, "written")
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else HERE)
+    main(sys.argv[1] if len(sys.argv) > 1 else HERE, set(sys.argv[2:]) or None)

@@ -139,13 +139,20 @@ def test_oracle_matches_reference_golden_vectors(path):
     o.set_psi(0.0, data["psi0"])
     if meta.get("normalize_first"):
         o.normalize_psi()
+    dipolar = meta.get("evolve") == "dipolar"
     for k, nsteps in enumerate(meta["steps"]):
-        mu = o.evolve_qf(nsteps)
+        mu = o.evolve_dipolar(nsteps) if dipolar else o.evolve_qf(nsteps)
         _, p = o.get_psi()
         ref = data[f"psi_{k}"]
         assert rel(p, ref) < meta["tol_psi"], (k, rel(p, ref))
         if meta["beta"] != 0:
             assert abs(mu - meta["mu"][k]) < 1e-10 * max(1.0, abs(meta["mu"][k]))
+    if meta.get("currents"):
+        _, jx, jy, jz = o.get_currents()
+        for a, j in zip("xyz", (jx, jy, jz)):
+            assert rel(j, data["j" + a]) < 1e-12, a
+    if dipolar:
+        assert o.energy_dipolar() == pytest.approx(meta["edip"], rel=1e-12)
     t, ek, ei, ee = o.energy()
     for a, b in zip((ek, ei, ee), meta["energy"]):
         assert abs(a - b) < 1e-10 * max(1.0, abs(b))

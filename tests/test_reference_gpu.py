@@ -23,6 +23,9 @@ CASES = [
     ((8, 32, 16), 0, 0.0, 1.0, 0.05, 1000.0, [0.04, 0.04, 0.06, 0.0], 0.1),
     ((16, 16, 16), 0, 1.0, 0.0, 0.05, 1000.0, [0.04, 0.04, 0.06, 0.0], 0.0),
     ((32, 32, 32), 0, 1.0, 0.0, 0.125, 1000.0, [0.04, 0.04, 0.06, 0.0], 0.1),
+    # BEC side of the crossover (INTERACTIONS 1), a_scat = 2
+    ((16, 16, 16), 1, 0.0, 1.0, 0.05, 100.0, [0.05, 0.05, 0.05, 2.0], 0.0),
+    ((16, 8, 32), 1, 1.0, 0.0, 0.05, 100.0, [0.05, 0.06, 0.04, 2.0], 0.1),
 ]
 
 
@@ -50,7 +53,7 @@ def engine_for(shape, inter, alpha, beta, dt, npart, params, qf, psi):
 @pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c[0]}_i{c[1]}_b{c[3]}_qf{c[7]}")
 def test_per_step_parity_with_reference(reference, gpe_lib, case):
     shape, inter, alpha, beta, dt, npart, params, qf = case
-    gamma = 1.0 if inter == -1 else 2.0
+    gamma = 1.0 if inter < 0 else 2.0
     psi = configs.random_state(shape, seed=21, npart=npart, gamma=gamma)
     # reference: 1 step, dump, 1 step, dump, ... ; ours restarts from the reference's psi each step
     cmds = []
@@ -71,7 +74,7 @@ def test_per_step_parity_with_reference(reference, gpe_lib, case):
 @pytest.mark.parametrize("case", CASES, ids=lambda c: f"{c[0]}_i{c[1]}_b{c[3]}_qf{c[7]}")
 def test_energy_density_after_n_steps(reference, gpe_lib, case):
     shape, inter, alpha, beta, dt, npart, params, qf = case
-    gamma = 1.0 if inter == -1 else 2.0
+    gamma = 1.0 if inter < 0 else 2.0
     psi = configs.random_state(shape, seed=22, npart=npart, gamma=gamma)
     n = 40
     out = ref_run.run(shape, inter, alpha, beta, dt, npart, params, psi, ["E", f"S{n}", "E", "D"], qf=qf)
@@ -134,7 +137,7 @@ def test_phase_enforcing_evolves_match_reference(reference, gpe_lib, beta, metho
 def test_currents_match_reference(reference, gpe_lib, case):
     """gpe_get_currents against the reference's own on the reference's state after 3 RTE steps."""
     shape, inter, alpha, beta, dt, npart, params, qf = case
-    gamma = 1.0 if inter == -1 else 2.0
+    gamma = 1.0 if inter < 0 else 2.0
     psi = configs.random_state(shape, seed=24, npart=npart, gamma=gamma)
     out = ref_run.run(shape, inter, 1.0, 0.0, dt, npart, params, psi, ["S3", "J", "D"], qf=qf)
     e = engine_for(shape, inter, 1.0, 0.0, dt, npart, params, qf, out["psi"][0])
