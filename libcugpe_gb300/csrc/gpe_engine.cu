@@ -1555,7 +1555,7 @@ int gpe_gb_set_quantum_friction_coeff(gpe_gb_engine* h, double q) {
 int gpe_gb_set_weizsacker(gpe_gb_engine* h, double lambda, double eps) {
     if (!h) return GPE_ERR_NO_ENGINE;
     Engine* e = &h->e;
-    // FP32 x pencils of 512 points hold 512-thread CTAs whose staged operands with
+    // FP32 x pencils of 512 points hold 8192-point CTAs whose staged operands with
     // the gradient sums exceed a CTA's shared memory
     if (lambda != 0.0 && e->prec == GPE_PRECISION_FP32 && e->n3[0] > 256) return GPE_ERR_LATTICE;
     e->wz = lambda;

@@ -110,7 +110,7 @@ template <> struct Plan<32> { static constexpr int E = 8, L = 2, R0 = 8, R1 = 4,
 template <> struct Plan<64> { static constexpr int E = 8, L = 2, R0 = 8, R1 = 8, R2 = 1; };
 template <> struct Plan<128> { static constexpr int E = 16, L = 2, R0 = 16, R1 = 8, R2 = 1; };
 template <> struct Plan<256> { static constexpr int E = 16, L = 2, R0 = 16, R1 = 16, R2 = 1; };
-template <> struct Plan<512> { static constexpr int E = 16, L = 3, R0 = 8, R1 = 8, R2 = 8; };
+template <> struct Plan<512> { static constexpr int E = 8, L = 3, R0 = 8, R1 = 8, R2 = 8; };
 
 template <int N, int S> __host__ __device__ constexpr int plan_rad() {
     return S == 0 ? Plan<N>::R0 : S == 1 ? Plan<N>::R1 : Plan<N>::R2;

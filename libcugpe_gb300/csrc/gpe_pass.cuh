@@ -319,15 +319,16 @@ template <typename R, int N, int AX, int NT> __host__ __device__ constexpr int p
 }
 
 // Geometry of one pass kernel instantiation.
-//  z pencils: a warp holds 32/T whole pencils, t fastest (coalesced rows).
+//  z pencils: t fastest (coalesced rows); a warp holds 32/T whole pencils, or
+//  one pencil spans T/32 warps (T > 32, 512 points).
 //  y/x pencils: a group of G = T*CW threads holds CW adjacent columns, column
 //  fastest, so a warp-wide access covers 32/T rows of CW contiguous points.
 template <typename R, int N, int AX, int NT>
 struct PassGeom {
     static constexpr int E = Plan<N>::E;
     static constexpr int T = N / E;
-    static constexpr int CW = (AX == AX_Z) ? (32 / T) : pass_cw<R, N, AX, NT>();
-    static constexpr int G = (AX == AX_Z) ? 32 : T * CW;
+    static constexpr int CW = (AX == AX_Z) ? ((32 / T) > 0 ? 32 / T : 1) : pass_cw<R, N, AX, NT>();
+    static constexpr int G = (AX == AX_Z) ? (T > 32 ? T : 32) : T * CW;
     static constexpr int W = NT / T;  // pencils per CTA
     static constexpr int ROW = padded_len<N>();
     static constexpr int TW = tw_len<N>();
@@ -343,8 +344,9 @@ struct PassGeom {
     // resident threads per SM the register allocation aims for: FP32 pencils up to 128 points fit
     // 7 CTAs of 128 threads in 72 registers without spills, 256-point ones 6 in 80, which runs the
     // 128^3 and 256^3 passes (1-2 waves of CTAs) in fewer rounds (measured: +8% RTE, +20% ITE
-    // steps/s at 128^3, +2% / +16% at 256^3); the 512-point passes were faster with 4
-    static constexpr int THREADS_SM = (sizeof(R) == 4) ? (N <= 128 ? 896 : N <= 256 ? 768 : 512) : 256;
+    // steps/s at 128^3, +2% / +16% at 256^3); 512-point pencils, at 8 points per thread, fit
+    // 1024 threads in 64 registers without spills
+    static constexpr int THREADS_SM = (sizeof(R) == 4) ? (N <= 128 ? 896 : N <= 256 ? 768 : 1024) : 256;
     static constexpr int MINB = (THREADS_SM / NT) > 0 ? THREADS_SM / NT : 1;
     static_assert(NT % G == 0 && NT % 32 == 0, "threads per CTA must hold whole groups");
     static_assert(SMEM_BASE + 2 * (size_t)E * NT * sizeof(C2<R>) <= SMEM_CAP,
@@ -405,9 +407,8 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     int pl, t, bar;
     C2<R>* sb;
     if constexpr (AX == AX_Z) {
-        const int w = tid >> 5, lane = tid & 31;
-        t = lane % T;
-        pl = w * CW + lane / T;
+        t = tid % T;
+        pl = tid / T;
         sb = sx + pl * ROW;
         bar = 0;
     } else {
@@ -858,9 +859,8 @@ __device__ __forceinline__ void kin_pipe_body(const PassArgs<R>& a) {
     int pl, t, bar;
     C2<R>* sb;
     if constexpr (AX == AX_Z) {
-        const int w = tid >> 5, lane = tid & 31;
-        t = lane % T;
-        pl = w * CW + lane / T;
+        t = tid % T;
+        pl = tid / T;
         sb = sx + pl * ROW;
         bar = 0;
     } else {
