@@ -424,7 +424,7 @@ def run_batch_workload(args):
                                        if any(done[j] for j, c in enumerate(ens) if c["shape"][0] == n) else None
                                        for n in sorted({c["shape"][0] for c in ens})},
             "unconverged": stragglers,
-            "config": {"workload": "config 3: BEC ITE, gN~U[50,500], omega_z/omega_perp~U[0.8,1.25], "
+            "config": {"workload": "ensemble of 96 BEC ITE solves (32 at 32^3, 48 at 64^3, 16 at 128^3), gN~U[50,500], omega_z/omega_perp~U[0.8,1.25], "
                                    "width~U[0.8,1.2], box 16 (dx=16/n), dt=5e-3; converged when the mean of mu over a "
                                    "25-step interval changes by < 1e-8 per step between intervals"}}
     print(json.dumps(line), flush=True)
@@ -450,7 +450,7 @@ def run_bec64_workload(args):
     line = {"metric": "64^3 BEC ITE steps/s (FP64 drop-in)", "value": w.steps / t_ours, "unit": "steps/s",
             "n_gpus": 1, "higher_is_better": True, "dtype": "f64", "data": "synthetic (seeded)",
             "mu": mu, "energy_per_particle": sum(en[1:]),
-            "config": {"workload": "config 1: 64^3, dx=0.25, omega=1, gN=100, ITE dt=1e-3, 2000 steps, "
+            "config": {"workload": "contact-BEC ITE ground state: 64^3, dx=0.25, omega=1, gN=100, ITE dt=1e-3, 2000 steps, "
                                    "Gaussian width 1 x (1+0.01u)"}}
     try:
         from oracle import build_ref, ref_run
@@ -520,8 +520,8 @@ def run_cool512_workload(args):
                                               "fp64_256_initial": f0 / w.npart, "fp64_256_final": f1 / w.npart,
                                               "final_rel_diff": abs(e1 - f1) / abs(f1)},
             "fp64_256_seconds": t64, "clocks": clk.summary(),
-            "config": {"workload": "config 5: 512^3, dx=0.1, UFG, quantum friction 0.2, omega=1, 8 vortex lines "
-                                   "(charge +1, seeded in the disk r<4), dt=2e-3, %d steps, npart=5e4 (not given)"
+            "config": {"workload": "cooling run: 512^3, dx=0.1, UFG, quantum friction 0.2, omega=1, 8 vortex lines "
+                                   "(charge +1, seeded in the disk r<4), dt=2e-3, %d steps, npart=5e4"
                                    % w.steps, "lattice": list(w.shape)}}
     print(json.dumps(line), flush=True)
 
@@ -582,7 +582,7 @@ def run_control_workload(args):
             "forward_plus_adjoint_seconds": t_grad, "grad_norm": float(np.linalg.norm(grad)),
             "fd_check": {"h": h, "controls": len(errs), "max_rel_err": max(e_["rel_err"] for e_ in errs),
                          "median_rel_err": float(np.median([e_["rel_err"] for e_ in errs])), "points": errs},
-            "config": {"workload": "config 4: 64^3, dx=0.25, gN=200, omega=1, dt=1e-3, 2000 steps, 16 Gaussians "
+            "config": {"workload": "optimal control of an RTE BEC: 64^3, dx=0.25, gN=200, omega=1, dt=1e-3, 2000 steps, 16 Gaussians "
                                    "sigma=0.8 centres U[-3,3]^3, 100 slices, controls N(0,0.05), target = ground state "
                                    "of the trap shifted by (0.5,0,0), checkpoints every 100 steps"}}
     print(json.dumps(line), flush=True)
