@@ -225,17 +225,30 @@ int gpe_gb_evolve_dipolar(gpe_gb_engine* e, int nt, double* chemical_potential);
 /* gpe_energy_dipolar2 (dev/gpe_engine.cu:1789-1809): E_dip = 1/2 sum rho vdip.
  * Also serves gpe_energy_dipolar (:1740), the same sum taken in k space. */
 int gpe_gb_energy_dipolar(gpe_gb_engine* e, double* t, double* edip);
+/* Radix plan of the pencil FFTs (no reference counterpart; replaces the
+ * choice cuFFT makes inside the reference's Z2Z plans, dev/gpe_engine.cu:343-350):
+ * 0 the default, 1 the alternative with the other point count per thread
+ * (8 <-> 16; more or fewer radix stages and threads per pencil), for FP32
+ * pencils of 32 to 512 points; FP64 engines and 8/16-point axes run plan 0
+ * (plan 1 on an FP64 engine: GPE_ERR_ARGUMENT).  Both plans compute the same
+ * transform; results differ only by FP32 rounding. */
+int gpe_gb_set_fft_plan(gpe_gb_engine* e, int plan);
+int gpe_gb_get_fft_plan(const gpe_gb_engine* e, int* plan);
+/* Plan of every condensate's passes in a batch (one plan per launch). */
+int gpe_gb_batch_set_fft_plan(gpe_gb_batch* b, int plan);
 /* Autotuner (no reference counterpart): times nsteps steps of the engine's
- * own state for each launch configuration it can run -- pass operands
- * staged in shared memory or read where used (FP32, pencils <= 128 points),
- * and 8, 16 or 32 steps per replayed CUDA graph -- keeps the fastest, and
- * puts psi, time and step counter back as they were.  Every configuration
- * computes bit-identical results.  Outputs (may be NULL): the chosen
- * operand mode (-1 when there is no choice), graph steps, ms per step. */
-int gpe_gb_autotune(gpe_gb_engine* e, int nsteps, int* direct, int* graph_steps, double* ms_per_step);
-/* The same for a batch: item order within each launch (0 as created, 1 the
- * condensates with most CTAs first) and steps per replayed graph. */
-int gpe_gb_batch_autotune(gpe_gb_batch* b, int nsteps, int* order, int* graph_steps, double* ms_per_step);
+ * own state for each launch configuration it can run -- FFT radix plan
+ * (FP32), pass operands staged in shared memory or read where used (FP32,
+ * pencils <= 128 points), and 8, 16 or 32 steps per replayed CUDA graph --
+ * keeps the fastest, and puts psi, time and step counter back as they were.
+ * Outputs (may be NULL): the chosen operand mode (-1 when there is no
+ * choice), graph steps, radix plan, ms per step. */
+int gpe_gb_autotune(gpe_gb_engine* e, int nsteps, int* direct, int* graph_steps, int* fft_plan,
+                    double* ms_per_step);
+/* The same for a batch: radix plan, item order within each launch (0 as
+ * created, 1 the condensates with most CTAs first) and steps per replayed graph. */
+int gpe_gb_batch_autotune(gpe_gb_batch* b, int nsteps, int* order, int* graph_steps, int* fft_plan,
+                          double* ms_per_step);
 /* Message for a return code. */
 const char* gpe_gb_error_string(int code);
 

@@ -50,6 +50,7 @@ C_ABI_SYMBOLS = [
     "gpe_gb_control_loss_grad", "gpe_gb_control_destroy", "gpe_gb_snapshots_open", "gpe_gb_snapshots_push",
     "gpe_gb_snapshots_close", "gpe_gb_dftc_write_info", "gpe_gb_dftc_read_info", "gpe_gb_set_weizsacker",
     "gpe_gb_evolve_dipolar", "gpe_gb_energy_dipolar", "gpe_gb_autotune", "gpe_gb_batch_autotune",
+    "gpe_gb_set_fft_plan", "gpe_gb_get_fft_plan", "gpe_gb_batch_set_fft_plan",
 ]
 
 
@@ -82,8 +83,11 @@ def _lib():
             "gpe_gb_set_quantum_friction_coeff": (i, [vp, d]),
             "gpe_gb_set_weizsacker": (i, [vp, d, d]),
             "gpe_gb_evolve_dipolar": (i, [vp, i, dp]),
-            "gpe_gb_autotune": (i, [vp, i, ip, ip, dp]),
-            "gpe_gb_batch_autotune": (i, [vp, i, ip, ip, dp]),
+            "gpe_gb_autotune": (i, [vp, i, ip, ip, ip, dp]),
+            "gpe_gb_batch_autotune": (i, [vp, i, ip, ip, ip, dp]),
+            "gpe_gb_set_fft_plan": (i, [vp, i]),
+            "gpe_gb_get_fft_plan": (i, [vp, ip]),
+            "gpe_gb_batch_set_fft_plan": (i, [vp, i]),
             "gpe_gb_energy_dipolar": (i, [vp, dp, dp]),
             "gpe_gb_set_psi": (i, [vp, d, dp]),
             "gpe_gb_get_psi": (i, [vp, dp, dp]),
@@ -255,11 +259,20 @@ class Engine:
 
     def autotune(self, nsteps=32):
         """Times each launch configuration on this engine's state and keeps the fastest; psi, time
-        and step counter are restored.  Returns {"direct", "graph_steps", "ms_per_step"}."""
-        d, c, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
-        _check(_lib().gpe_gb_autotune(self._h, int(nsteps), ctypes.byref(d), ctypes.byref(c), ctypes.byref(ms)),
-               "autotune")
-        return {"direct": d.value, "graph_steps": c.value, "ms_per_step": ms.value}
+        and step counter are restored.  Returns {"direct", "graph_steps", "fft_plan", "ms_per_step"}."""
+        d, c, p, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        _check(_lib().gpe_gb_autotune(self._h, int(nsteps), ctypes.byref(d), ctypes.byref(c), ctypes.byref(p),
+                                      ctypes.byref(ms)), "autotune")
+        return {"direct": d.value, "graph_steps": c.value, "fft_plan": p.value, "ms_per_step": ms.value}
+
+    def set_fft_plan(self, plan):
+        """Radix plan of the pencil FFTs: 0 default, 1 the alternative (FP32, pencils of 32-512 points)."""
+        _check(_lib().gpe_gb_set_fft_plan(self._h, int(plan)), "set_fft_plan")
+
+    def get_fft_plan(self):
+        p = ctypes.c_int()
+        _check(_lib().gpe_gb_get_fft_plan(self._h, ctypes.byref(p)), "get_fft_plan")
+        return p.value
 
     def evolve_dipolar(self, nt):
         """gpe_evolve_dipolar: nt steps of the dipolar BEC (interactions -2); mu in ITE."""
@@ -373,10 +386,14 @@ class Batch:
 
     def autotune(self, nsteps=32):
         """Item order and graph length of the batched passes, timed on the batch's state (restored)."""
-        o, c, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        o, c, p, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
         _check(_lib().gpe_gb_batch_autotune(self._h, int(nsteps), ctypes.byref(o), ctypes.byref(c),
-                                            ctypes.byref(ms)), "batch_autotune")
-        return {"order": o.value, "graph_steps": c.value, "ms_per_step": ms.value}
+                                            ctypes.byref(p), ctypes.byref(ms)), "batch_autotune")
+        return {"order": o.value, "graph_steps": c.value, "fft_plan": p.value, "ms_per_step": ms.value}
+
+    def set_fft_plan(self, plan):
+        """Radix plan of every condensate's pencil FFTs (0 default, 1 alternative)."""
+        _check(_lib().gpe_gb_batch_set_fft_plan(self._h, int(plan)), "batch_set_fft_plan")
 
     def chemical_potentials(self):
         """Per condensate: (mu of the last ITE step, running sum of mu)."""

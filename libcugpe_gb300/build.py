@@ -30,15 +30,17 @@ def _sources():
     gen = os.path.join(BUILD, "gen")
     os.makedirs(gen, exist_ok=True)
     units = []
-    for tag, ctype in PRECISIONS.items():
-        for n in LENGTHS:
-            path = os.path.join(gen, f"pass_{tag}_{n}.cu")
-            text = ('#define GPE_PASS_DEFINITIONS\n#include "gpe_launch.cuh"\n'
-                    f"GPE_INSTANTIATE_N({ctype}, {n})\n")
-            if not os.path.isfile(path) or open(path).read() != text:
-                with open(path, "w") as fh:
-                    fh.write(text)
-            units.append(path)
+    # radix plan 0 for every (precision, length); the alternative plan 1 for FP32 pencils of 32-512 points
+    combos = [(tag, ctype, n, 0) for tag, ctype in PRECISIONS.items() for n in LENGTHS]
+    combos += [("f32", "float", n, 1) for n in LENGTHS if n >= 32]
+    for tag, ctype, n, plan in combos:
+        path = os.path.join(gen, f"pass_{tag}_{n}" + (f"_p{plan}" if plan else "") + ".cu")
+        text = ('#define GPE_PASS_DEFINITIONS\n#include "gpe_launch.cuh"\n'
+                f"GPE_INSTANTIATE_N({ctype}, {n}, {plan})\n")
+        if not os.path.isfile(path) or open(path).read() != text:
+            with open(path, "w") as fh:
+                fh.write(text)
+        units.append(path)
     units.append(os.path.join(CSRC, "gpe_engine.cu"))
     units.append(os.path.join(CSRC, "gpe_noalloc.cu"))
     units.append(os.path.join(CSRC, "gpe_batch_kernels.cu"))

@@ -2,7 +2,7 @@
 // in a batch, whatever its lattice size.  CTA b finds its condensate by a
 // binary search over the items' first-CTA offsets and runs the pass body for
 // that condensate's pencil length (32, 64, 128 or 256 points, all with
-// 128-thread CTAs).  Each condensate keeps its own tables, device state and
+// 128-thread CTAs) under the batch's radix plan P.  Each condensate keeps its own tables, device state and
 // reduction slots, so the last-CTA reductions stay per condensate.
 #pragma once
 #include <cuda_runtime.h>
@@ -20,10 +20,12 @@ struct BatchItem {
 };
 
 constexpr int kBatchThreads = 128;
+// 7 CTAs per SM: the register budget (72) that the 32- to 128-point bodies of either plan fit
+constexpr int kBatchMinBlocks = 7;
 constexpr int kBatchLengths[4] = {32, 64, 128, 256};
 
-template <typename R, int AX, int CLS>
-__global__ void __launch_bounds__(kBatchThreads, PassGeom<R, 128, AX, kBatchThreads>::MINB)
+template <typename R, int AX, int CLS, int P>
+__global__ void __launch_bounds__(kBatchThreads, kBatchMinBlocks)
 pass_batch_kernel(const BatchItem<R>* __restrict__ items, int nitems) {
     int lo = 0, hi = nitems - 1;
     while (lo < hi) {
@@ -34,20 +36,20 @@ pass_batch_kernel(const BatchItem<R>* __restrict__ items, int nitems) {
     const BatchItem<R>& it = items[lo];
     const uint32_t blk = blockIdx.x - it.cta_begin;
     switch (it.n) {
-        case 32: pass_body<R, 32, AX, kBatchThreads, CLS>(it.a, blk, it.nctas); break;
-        case 64: pass_body<R, 64, AX, kBatchThreads, CLS>(it.a, blk, it.nctas); break;
-        case 128: pass_body<R, 128, AX, kBatchThreads, CLS>(it.a, blk, it.nctas); break;
-        default: pass_body<R, 256, AX, kBatchThreads, CLS>(it.a, blk, it.nctas); break;
+        case 32: pass_body<R, 32, AX, kBatchThreads, CLS, P>(it.a, blk, it.nctas); break;
+        case 64: pass_body<R, 64, AX, kBatchThreads, CLS, P>(it.a, blk, it.nctas); break;
+        case 128: pass_body<R, 128, AX, kBatchThreads, CLS, P>(it.a, blk, it.nctas); break;
+        default: pass_body<R, 256, AX, kBatchThreads, CLS, P>(it.a, blk, it.nctas); break;
     }
 }
 
 // CTAs and dynamic shared memory of one condensate's pass in a batch.
-template <typename R, int AX>
+template <typename R, int AX, int P>
 inline bool batch_shape(int n, size_t pencils, uint32_t ops, uint32_t* nctas, size_t* smem) {
     switch (n) {
 #define GPE_BATCH_CASE(NN)                                                                      \
     case NN: {                                                                                  \
-        using Geo = PassGeom<R, NN, AX, kBatchThreads>;                                         \
+        using Geo = PassGeom<R, NN, AX, kBatchThreads, P>;                                      \
         *nctas = (uint32_t)((pencils + Geo::W - 1) / Geo::W);                                   \
         *smem = Geo::SMEM_BASE + slot_bytes<R>(ops, Geo::E * kBatchThreads);                    \
         return true;                                                                            \
@@ -62,7 +64,7 @@ inline bool batch_shape(int n, size_t pencils, uint32_t ops, uint32_t* nctas, si
 }
 
 template <typename R>
-cudaError_t launch_batch(int axis, int cls, const BatchItem<R>* items, int nitems, unsigned grid, size_t smem,
-                         cudaStream_t st);
+cudaError_t launch_batch(int axis, int cls, int plan, const BatchItem<R>* items, int nitems, unsigned grid,
+                         size_t smem, cudaStream_t st);
 
 }  // namespace gpe

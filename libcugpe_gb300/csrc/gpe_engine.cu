@@ -189,7 +189,7 @@ struct AxisTables {
     void* ktab;   // C2<R>[N]  exp(c3 k^2 / Gamma^2) / N
     void* lqf;    // R[N]      k^2 / N   (second derivative; friction and Weizsaecker terms)
     void* lek;    // R[N]      k^2 / (2 Gamma) / N
-    void* tw;     // C2<R>[tw_len]  stage-major twiddles (gpe_fft.cuh)
+    void* tw[2];  // C2<R>[tw_len]  stage-major twiddles of radix plans 0 and 1 (gpe_fft.cuh)
     void* vt;     // R[N]      0.5 i^2 w^2, i = index - N/2
     void* lcur;   // R[N]      k / (Gamma N)   (probability currents)
     void* ld1;    // R[N]      k / N           (first derivative, Weizsaecker term)
@@ -230,6 +230,7 @@ struct Engine {
     bool use_graph = true;
     int direct_mode = -1;   // operands read where used: -1 by lattice size, 0 staged, 1 direct (autotuner)
     int graph_chunk = 16;   // steps per replayed graph (autotuner)
+    int fft_plan = 0;       // radix plan of the pencil FFTs: 0 default, 1 alternative (FP32; autotuner)
     bool graph_dirty = true;
     unsigned version = 0;  // bumped whenever tables or captured arguments change
     bool lap_valid = false;  // lap holds the z-Laplacian term of the current psi
@@ -273,23 +274,27 @@ static void step_coeff(const Engine* e, double* c3x, double* c3y) {
     *c3y = -a * bi / den;
 }
 
-template <int N> static void plan_of(int rad[3], int* L) {
-    rad[0] = Plan<N>::R0; rad[1] = Plan<N>::R1; rad[2] = Plan<N>::R2; *L = Plan<N>::L;
+template <int N, int P> static void plan_of(int rad[3], int* L) {
+    rad[0] = Plan<N, P>::R0; rad[1] = Plan<N, P>::R1; rad[2] = Plan<N, P>::R2; *L = Plan<N, P>::L;
+}
+template <int N> static void plan_of(int P, int rad[3], int* L) {
+    if (P == 1) plan_of<N, 1>(rad, L);
+    else plan_of<N, 0>(rad, L);
 }
 
-// Stage-major twiddles: stage s (Ns > 1) holds exp(-2 pi i r k / (Ns R)) at
+// Stage-major twiddles of radix plan P: stage s (Ns > 1) holds exp(-2 pi i r k / (Ns R)) at
 // r*Ns + k, stages packed in order (layout of tw_off / tw_len).
 template <typename R>
-static void stage_twiddles(int N, C2<R>* tw) {
+static void stage_twiddles(int N, int P, C2<R>* tw) {
     int rad[3] = {1, 1, 1}, L = 1;
     switch (N) {
-        case 8: plan_of<8>(rad, &L); break;
-        case 16: plan_of<16>(rad, &L); break;
-        case 32: plan_of<32>(rad, &L); break;
-        case 64: plan_of<64>(rad, &L); break;
-        case 128: plan_of<128>(rad, &L); break;
-        case 256: plan_of<256>(rad, &L); break;
-        default: plan_of<512>(rad, &L); break;
+        case 8: plan_of<8>(P, rad, &L); break;
+        case 16: plan_of<16>(P, rad, &L); break;
+        case 32: plan_of<32>(P, rad, &L); break;
+        case 64: plan_of<64>(P, rad, &L); break;
+        case 128: plan_of<128>(P, rad, &L); break;
+        case 256: plan_of<256>(P, rad, &L); break;
+        default: plan_of<512>(P, rad, &L); break;
     }
     int off = 0, ns = rad[0];
     tw[0].x = (R)1; tw[0].y = (R)0;
@@ -315,7 +320,7 @@ static int upload_tables(Engine* e) {
     size_t off = 0;
     std::vector<unsigned char> host;
     size_t total = 0;
-    for (int a = 0; a < 3; a++) total += (size_t)e->n3[a] * (3 * sizeof(C2<R>) + 6 * sizeof(R)) + 256 * 8;
+    for (int a = 0; a < 3; a++) total += (size_t)e->n3[a] * (5 * sizeof(C2<R>) + 6 * sizeof(R)) + 256 * 9;
     host.assign(total, 0);
     if (!e->tabmem) GPE_CK(cudaMalloc(&e->tabmem, total));
     unsigned char* dbase = (unsigned char*)e->tabmem;
@@ -325,7 +330,8 @@ static int upload_tables(Engine* e) {
         std::vector<double> k;
         kgrid(k, N);
         const size_t okt = take(N * sizeof(C2<R>)), olq = take(N * sizeof(R)), ole = take(N * sizeof(R)),
-                     otw = take(2 * N * sizeof(C2<R>)), ovt = take(N * sizeof(R)), ocu = take(N * sizeof(R)),
+                     otw = take(2 * N * sizeof(C2<R>)), otw1 = take(2 * N * sizeof(C2<R>)),
+                     ovt = take(N * sizeof(R)), ocu = take(N * sizeof(R)),
                      od1 = take(N * sizeof(R)), okk = take(N * sizeof(R));
         C2<R>* kt = (C2<R>*)(host.data() + okt);
         R* lq = (R*)(host.data() + olq);
@@ -353,8 +359,10 @@ static int upload_tables(Engine* e) {
             kq[i] = (R)k[i];
         }
         e->ax[a].ktab = dbase + okt; e->ax[a].lqf = dbase + olq; e->ax[a].lek = dbase + ole;
-        stage_twiddles<R>(N, tw);
-        e->ax[a].tw = dbase + otw; e->ax[a].vt = dbase + ovt; e->ax[a].lcur = dbase + ocu;
+        stage_twiddles<R>(N, 0, tw);
+        stage_twiddles<R>(N, has_plan1(N) ? 1 : 0, (C2<R>*)(host.data() + otw1));
+        e->ax[a].tw[0] = dbase + otw; e->ax[a].tw[1] = dbase + otw1;
+        e->ax[a].vt = dbase + ovt; e->ax[a].lcur = dbase + ocu;
         e->ax[a].ld1 = dbase + od1;
         e->ax[a].kk = dbase + okk;
     }
@@ -485,7 +493,8 @@ static PassArgs<R> base_args(const Engine* e) {
 template <typename R>
 static void axis_args(const Engine* e, PassArgs<R>& a, int axis) {
     a.ktab = (const C2<R>*)e->ax[axis].ktab;
-    a.tw = (const C2<R>*)e->ax[axis].tw;
+    a.plan = effective_plan(e->fft_plan, e->n3[axis], e->prec == GPE_PRECISION_FP32);
+    a.tw = (const C2<R>*)e->ax[axis].tw[a.plan];
     a.ld1 = (const R*)e->ax[axis].ld1;
 }
 
@@ -1296,7 +1305,7 @@ struct gpe_gb_batch {
     cudaStream_t st = nullptr;
     struct Launch {
         void* items = nullptr;
-        int nitems = 0, axis = 0, cls = 0;
+        int nitems = 0, axis = 0, cls = 0, plan = 0;
         unsigned grid = 0;
         size_t smem = 0;
     };
@@ -1307,6 +1316,7 @@ struct gpe_gb_batch {
     long long launches = 0;
     int order = 0;    // item order in a launch: 0 as created, 1 most CTAs first (autotuner)
     int chunk = 16;   // steps per replayed graph (autotuner)
+    int plan = 0;     // radix plan of every condensate's pencil FFTs (autotuner)
 };
 
 namespace gpe {
@@ -1320,8 +1330,9 @@ static void batch_free_items(gpe_gb_batch* b) {
 }
 
 template <int AX>
-static bool batch_shape_axis(int n, size_t pencils, uint32_t ops, uint32_t* nctas, size_t* smem) {
-    return batch_shape<float, AX>(n, pencils, ops, nctas, smem);
+static bool batch_shape_axis(int plan, int n, size_t pencils, uint32_t ops, uint32_t* nctas, size_t* smem) {
+    return plan == 1 ? batch_shape<float, AX, 1>(n, pencils, ops, nctas, smem)
+                     : batch_shape<float, AX, 0>(n, pencils, ops, nctas, smem);
 }
 
 static int batch_build(gpe_gb_batch* b) {
@@ -1343,12 +1354,16 @@ static int batch_build(gpe_gb_batch* b) {
             it.a = desc_args<float>(e, d);
             it.a.flags &= ~F_DIRECT;  // the batched pass compiles the staged classes only
             it.n = e->n3[d.axis];
+            if (effective_plan(b->plan, it.n, true) != b->plan) return GPE_ERR_LATTICE;
+            it.a.plan = b->plan;  // one plan per batched launch: the batch's, with its twiddles
+            it.a.tw = (const C2<float>*)e->ax[d.axis].tw[b->plan];
             uint32_t nctas = 0;
             size_t sm = 0;
             const uint32_t ops = staged_ops(d.mid, d.post, it.a.flags);
-            const bool ok = (d.axis == AX_X) ? batch_shape_axis<AX_X>(it.n, it.a.npencils, ops, &nctas, &sm)
-                          : (d.axis == AX_Y) ? batch_shape_axis<AX_Y>(it.n, it.a.npencils, ops, &nctas, &sm)
-                                             : batch_shape_axis<AX_Z>(it.n, it.a.npencils, ops, &nctas, &sm);
+            const int pl = b->plan;
+            const bool ok = (d.axis == AX_X) ? batch_shape_axis<AX_X>(pl, it.n, it.a.npencils, ops, &nctas, &sm)
+                          : (d.axis == AX_Y) ? batch_shape_axis<AX_Y>(pl, it.n, it.a.npencils, ops, &nctas, &sm)
+                                             : batch_shape_axis<AX_Z>(pl, it.n, it.a.npencils, ops, &nctas, &sm);
             if (!ok) return GPE_ERR_LATTICE;
             it.nctas = nctas;
             if (sm > smem) smem = sm;
@@ -1365,6 +1380,7 @@ static int batch_build(gpe_gb_batch* b) {
         gpe_gb_batch::Launch l;
         l.nitems = (int)items.size();
         l.axis = d.axis;
+        l.plan = b->plan;
         l.cls = op_class(d.pre, d.mid, d.post, items[0].a.flags);
         l.grid = cta;
         l.smem = smem;
@@ -1380,8 +1396,8 @@ static int batch_build(gpe_gb_batch* b) {
 static int batch_steps(gpe_gb_batch* b, int k) {
     for (int i = 0; i < k; i++)
         for (const auto& l : b->passes) {
-            GPE_CK(launch_batch<float>(l.axis, l.cls, (const BatchItem<float>*)l.items, l.nitems, l.grid, l.smem,
-                                       b->st));
+            GPE_CK(launch_batch<float>(l.axis, l.cls, l.plan, (const BatchItem<float>*)l.items, l.nitems, l.grid,
+                                       l.smem, b->st));
             b->launches++;
         }
     return 0;
@@ -2027,42 +2043,71 @@ int gpe_gb_control_destroy(gpe_gb_control* hc) {
     return gpe::cuda_rc(cudaGetLastError());
 }
 
-int gpe_gb_autotune(gpe_gb_engine* h, int nsteps, int* direct, int* chunk, double* ms_per_step) {
+int gpe_gb_set_fft_plan(gpe_gb_engine* h, int plan) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    Engine* e = &h->e;
+    if (plan != 0 && plan != 1) return GPE_ERR_ARGUMENT;
+    if (plan == 1 && e->prec != GPE_PRECISION_FP32) return GPE_ERR_ARGUMENT;
+    if (plan != e->fft_plan) {
+        e->fft_plan = plan;
+        gpe::drop_graph(e);
+        e->graph_dirty = true;
+        e->version++;  // batches holding this engine rebuild their launches
+    }
+    return 0;
+}
+
+int gpe_gb_get_fft_plan(const gpe_gb_engine* h, int* plan) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    if (!plan) return GPE_ERR_ARGUMENT;
+    *plan = h->e.fft_plan;
+    return 0;
+}
+
+int gpe_gb_autotune(gpe_gb_engine* h, int nsteps, int* direct, int* chunk, int* fft_plan, double* ms_per_step) {
     if (!h) return GPE_ERR_NO_ENGINE;
     Engine* e = &h->e;
     if (nsteps < 4) nsteps = 4;
     gpe::Snap snap;
     GPE_RC(gpe::snap_save(e, &snap));
+    const bool fp32 = e->prec == GPE_PRECISION_FP32;
     const bool small_axis = e->n3[0] <= 128 || e->n3[1] <= 128 || e->n3[2] <= 128;
-    const int nd = (e->prec == GPE_PRECISION_FP32 && small_axis) ? 2 : 1;
+    const bool alt_plan = fp32 && (gpe::has_plan1(e->n3[0]) || gpe::has_plan1(e->n3[1]) || gpe::has_plan1(e->n3[2]));
+    const int nd = (fp32 && small_axis) ? 2 : 1;
+    const int np = alt_plan ? 2 : 1;
     const int chunks[3] = {8, 16, 32};
     double best = 1e300;
-    int bd = 0, bc = 16, rc = 0;
+    int bd = 0, bc = 16, bp = 0, rc = 0;
     cudaEvent_t a = nullptr, b = nullptr;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
-    for (int d = 0; d < nd && !rc; d++) {
-        for (int c = 0; c < 3 && !rc; c++) {
-            e->direct_mode = d;
-            e->graph_chunk = chunks[c];
-            gpe::drop_graph(e);
-            e->graph_dirty = true;
-            if ((rc = gpe::snap_load(e, &snap))) break;
-            if ((rc = gpe::evolve(e, nsteps, nullptr))) break;  // builds the graph
-            if ((rc = gpe::snap_load(e, &snap))) break;
-            cudaEventRecord(a, e->st);
-            if ((rc = gpe::evolve(e, nsteps, nullptr))) break;
-            cudaEventRecord(b, e->st);
-            cudaEventSynchronize(b);
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, a, b);
-            if (ms < best) { best = ms; bd = d; bc = chunks[c]; }
+    for (int p = 0; p < np && !rc; p++) {
+        for (int d = 0; d < nd && !rc; d++) {
+            for (int c = 0; c < 3 && !rc; c++) {
+                e->fft_plan = p;
+                e->direct_mode = d;
+                e->graph_chunk = chunks[c];
+                gpe::drop_graph(e);
+                e->graph_dirty = true;
+                if ((rc = gpe::snap_load(e, &snap))) break;
+                if ((rc = gpe::evolve(e, nsteps, nullptr))) break;  // builds the graph
+                if ((rc = gpe::snap_load(e, &snap))) break;
+                cudaEventRecord(a, e->st);
+                if ((rc = gpe::evolve(e, nsteps, nullptr))) break;
+                cudaEventRecord(b, e->st);
+                cudaEventSynchronize(b);
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, a, b);
+                if (ms < best) { best = ms; bd = d; bc = chunks[c]; bp = p; }
+            }
         }
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
+    e->fft_plan = bp;
     e->direct_mode = (nd == 2) ? bd : -1;
     e->graph_chunk = bc;
+    e->version++;
     gpe::drop_graph(e);
     e->graph_dirty = true;
     const int rc2 = gpe::snap_load(e, &snap);
@@ -2071,11 +2116,23 @@ int gpe_gb_autotune(gpe_gb_engine* h, int nsteps, int* direct, int* chunk, doubl
     if (rc2) return rc2;
     if (direct) *direct = e->direct_mode;
     if (chunk) *chunk = e->graph_chunk;
+    if (fft_plan) *fft_plan = e->fft_plan;
     if (ms_per_step) *ms_per_step = best / nsteps;
     return 0;
 }
 
-int gpe_gb_batch_autotune(gpe_gb_batch* bt, int nsteps, int* order, int* chunk, double* ms_per_step) {
+int gpe_gb_batch_set_fft_plan(gpe_gb_batch* bt, int plan) {
+    if (!bt) return GPE_ERR_ARGUMENT;
+    if (plan != 0 && plan != 1) return GPE_ERR_ARGUMENT;
+    if (plan != bt->plan) {
+        bt->plan = plan;
+        bt->dirty = true;
+    }
+    return 0;
+}
+
+int gpe_gb_batch_autotune(gpe_gb_batch* bt, int nsteps, int* order, int* chunk, int* fft_plan,
+                          double* ms_per_step) {
     if (!bt) return GPE_ERR_ARGUMENT;
     if (nsteps < 4) nsteps = 4;
     std::vector<gpe::Snap> snaps(bt->eng.size());
@@ -2087,29 +2144,33 @@ int gpe_gb_batch_autotune(gpe_gb_batch* bt, int nsteps, int* order, int* chunk, 
     };
     const int chunks[3] = {8, 16, 32};
     double best = 1e300;
-    int bo = 0, bc = 16;
+    int bo = 0, bc = 16, bp = 0;
     cudaEvent_t a = nullptr, b = nullptr;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
-    for (int o = 0; o < 2 && !rc; o++) {
-        for (int c = 0; c < 3 && !rc; c++) {
-            bt->order = o;
-            bt->chunk = chunks[c];
-            bt->dirty = true;
-            if ((rc = restore())) break;
-            if ((rc = gpe::batch_evolve(bt, nsteps))) break;  // builds items and graph
-            if ((rc = restore())) break;
-            cudaEventRecord(a, bt->st);
-            if ((rc = gpe::batch_evolve(bt, nsteps))) break;
-            cudaEventRecord(b, bt->st);
-            cudaEventSynchronize(b);
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, a, b);
-            if (ms < best) { best = ms; bo = o; bc = chunks[c]; }
+    for (int p = 0; p < 2 && !rc; p++) {
+        for (int o = 0; o < 2 && !rc; o++) {
+            for (int c = 0; c < 3 && !rc; c++) {
+                bt->plan = p;
+                bt->order = o;
+                bt->chunk = chunks[c];
+                bt->dirty = true;
+                if ((rc = restore())) break;
+                if ((rc = gpe::batch_evolve(bt, nsteps))) break;  // builds items and graph
+                if ((rc = restore())) break;
+                cudaEventRecord(a, bt->st);
+                if ((rc = gpe::batch_evolve(bt, nsteps))) break;
+                cudaEventRecord(b, bt->st);
+                cudaEventSynchronize(b);
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, a, b);
+                if (ms < best) { best = ms; bo = o; bc = chunks[c]; bp = p; }
+            }
         }
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
+    bt->plan = bp;
     bt->order = bo;
     bt->chunk = bc;
     bt->dirty = true;
@@ -2119,6 +2180,7 @@ int gpe_gb_batch_autotune(gpe_gb_batch* bt, int nsteps, int* order, int* chunk, 
     if (rc2) return rc2;
     if (order) *order = bo;
     if (chunk) *chunk = bc;
+    if (fft_plan) *fft_plan = bp;
     if (ms_per_step) *ms_per_step = best / nsteps;
     return 0;
 }

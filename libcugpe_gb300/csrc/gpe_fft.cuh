@@ -103,32 +103,43 @@ __device__ __forceinline__ void dft(C2<R> (&u)[RAD]) {
 
 // ---------------------------------------------------------------- plans
 // Radix sequence per pencil length; E = points per thread, T = threads per pencil.
-template <int N> struct Plan;
-template <> struct Plan<8> { static constexpr int E = 8, L = 1, R0 = 8, R1 = 1, R2 = 1; };
-template <> struct Plan<16> { static constexpr int E = 16, L = 1, R0 = 16, R1 = 1, R2 = 1; };
-template <> struct Plan<32> { static constexpr int E = 8, L = 2, R0 = 8, R1 = 4, R2 = 1; };
-template <> struct Plan<64> { static constexpr int E = 8, L = 2, R0 = 8, R1 = 8, R2 = 1; };
-template <> struct Plan<128> { static constexpr int E = 16, L = 2, R0 = 16, R1 = 8, R2 = 1; };
-template <> struct Plan<256> { static constexpr int E = 16, L = 2, R0 = 16, R1 = 16, R2 = 1; };
-template <> struct Plan<512> { static constexpr int E = 8, L = 3, R0 = 8, R1 = 8, R2 = 8; };
+// Plan<N, 0> is the default; Plan<N, 1> runs the same pencil with the other
+// point count per thread (8 <-> 16), an alternative the autotuner may pick
+// for FP32 lattices (pencils of 32 to 512 points).
+template <int N> struct Plan0;
+template <> struct Plan0<8> { static constexpr int E = 8, L = 1, R0 = 8, R1 = 1, R2 = 1; };
+template <> struct Plan0<16> { static constexpr int E = 16, L = 1, R0 = 16, R1 = 1, R2 = 1; };
+template <> struct Plan0<32> { static constexpr int E = 8, L = 2, R0 = 8, R1 = 4, R2 = 1; };
+template <> struct Plan0<64> { static constexpr int E = 8, L = 2, R0 = 8, R1 = 8, R2 = 1; };
+template <> struct Plan0<128> { static constexpr int E = 16, L = 2, R0 = 16, R1 = 8, R2 = 1; };
+template <> struct Plan0<256> { static constexpr int E = 16, L = 2, R0 = 16, R1 = 16, R2 = 1; };
+template <> struct Plan0<512> { static constexpr int E = 8, L = 3, R0 = 8, R1 = 8, R2 = 8; };
 
-template <int N, int S> __host__ __device__ constexpr int plan_rad() {
-    return S == 0 ? Plan<N>::R0 : S == 1 ? Plan<N>::R1 : Plan<N>::R2;
+template <int N, int P = 0> struct Plan : Plan0<N> {};
+template <> struct Plan<32, 1> { static constexpr int E = 16, L = 2, R0 = 16, R1 = 2, R2 = 1; };
+template <> struct Plan<64, 1> { static constexpr int E = 16, L = 2, R0 = 16, R1 = 4, R2 = 1; };
+template <> struct Plan<128, 1> { static constexpr int E = 8, L = 3, R0 = 8, R1 = 8, R2 = 2; };
+template <> struct Plan<256, 1> { static constexpr int E = 8, L = 3, R0 = 8, R1 = 8, R2 = 4; };
+template <> struct Plan<512, 1> { static constexpr int E = 16, L = 3, R0 = 8, R1 = 8, R2 = 8; };
+__host__ __device__ constexpr bool has_plan1(int n) { return n >= 32 && n <= 512; }
+
+template <int N, int P, int S> __host__ __device__ constexpr int plan_rad() {
+    return S == 0 ? Plan<N, P>::R0 : S == 1 ? Plan<N, P>::R1 : Plan<N, P>::R2;
 }
-template <int N, int S> __host__ __device__ constexpr int plan_ns() {
-    return S == 0 ? 1 : S == 1 ? Plan<N>::R0 : Plan<N>::R0 * Plan<N>::R1;
+template <int N, int P, int S> __host__ __device__ constexpr int plan_ns() {
+    return S == 0 ? 1 : S == 1 ? Plan<N, P>::R0 : Plan<N, P>::R0 * Plan<N, P>::R1;
 }
 
 // Stage-major twiddle table: stage S (Ns > 1) owns RAD*Ns entries at
-// tw_off<N, S>(), entry r*Ns + k = exp(-2 pi i r k / (Ns RAD)), so the lanes of
+// tw_off<N, P, S>(), entry r*Ns + k = exp(-2 pi i r k / (Ns RAD)), so the lanes of
 // a stage (consecutive k) read consecutive entries.
-template <int N, int S> __host__ __device__ constexpr int tw_off() {
-    return (S <= 1) ? 0 : plan_rad<N, 1>() * plan_ns<N, 1>();
+template <int N, int P, int S> __host__ __device__ constexpr int tw_off() {
+    return (S <= 1) ? 0 : plan_rad<N, P, 1>() * plan_ns<N, P, 1>();
 }
-template <int N> __host__ __device__ constexpr int tw_len() {
-    return (Plan<N>::L == 1) ? 1
-         : (Plan<N>::L == 2) ? plan_rad<N, 1>() * plan_ns<N, 1>()
-         : plan_rad<N, 1>() * plan_ns<N, 1>() + plan_rad<N, 2>() * plan_ns<N, 2>();
+template <int N, int P> __host__ __device__ constexpr int tw_len() {
+    return (Plan<N, P>::L == 1) ? 1
+         : (Plan<N, P>::L == 2) ? plan_rad<N, P, 1>() * plan_ns<N, P, 1>()
+         : plan_rad<N, P, 1>() * plan_ns<N, P, 1>() + plan_rad<N, P, 2>() * plan_ns<N, P, 2>();
 }
 
 // Exchange layout: point p of a pencil sits at padp(p) * SSTR, one padding
@@ -154,11 +165,11 @@ template <int G> __device__ __forceinline__ void group_sync(int bar) {
 // thread's pencil in shared memory (point p at sb[padp(p) * SSTR]); `tw` is
 // the stage-major twiddle table (tw_off / tw_len).  The last stage keeps its
 // result in registers; the others exchange through `sb`.
-template <typename R, int N, int S, bool INV, int SSTR, int G>
-__device__ __forceinline__ void stage(C2<R> (&v)[Plan<N>::E], C2<R>* sb, int t, const C2<R>* tw, int bar) {
-    constexpr int E = Plan<N>::E, T = N / E, L = Plan<N>::L;
-    constexpr int RAD = plan_rad<N, S>();
-    constexpr int NS = plan_ns<N, S>();
+template <typename R, int N, int P, int S, bool INV, int SSTR, int G>
+__device__ __forceinline__ void stage(C2<R> (&v)[Plan<N, P>::E], C2<R>* sb, int t, const C2<R>* tw, int bar) {
+    constexpr int E = Plan<N, P>::E, T = N / E, L = Plan<N, P>::L;
+    constexpr int RAD = plan_rad<N, P, S>();
+    constexpr int NS = plan_ns<N, P, S>();
     constexpr int MB = E / RAD;
     constexpr bool LAST = (S == L - 1);
     if constexpr (!LAST) group_sync<G>(bar);  // earlier readers of sb are done
@@ -172,7 +183,7 @@ __device__ __forceinline__ void stage(C2<R> (&v)[Plan<N>::E], C2<R>* sb, int t, 
         if constexpr (NS > 1) {
 #pragma unroll
             for (int r = 1; r < RAD; r++) {
-                C2<R> w = tw[tw_off<N, S>() + r * NS + k];
+                C2<R> w = tw[tw_off<N, P, S>() + r * NS + k];
                 if constexpr (INV) w.y = -w.y;
                 u[r] = cmul(u[r], w);
             }
@@ -195,11 +206,11 @@ __device__ __forceinline__ void stage(C2<R> (&v)[Plan<N>::E], C2<R>* sb, int t, 
 }
 
 // Unnormalised transform, forward (exp(-2 pi i jk/N)) or inverse (exp(+...)).
-template <typename R, int N, bool INV, int SSTR, int G>
-__device__ __forceinline__ void fft(C2<R> (&v)[Plan<N>::E], C2<R>* sb, int t, const C2<R>* tw, int bar) {
-    stage<R, N, 0, INV, SSTR, G>(v, sb, t, tw, bar);
-    if constexpr (Plan<N>::L > 1) stage<R, N, 1, INV, SSTR, G>(v, sb, t, tw, bar);
-    if constexpr (Plan<N>::L > 2) stage<R, N, 2, INV, SSTR, G>(v, sb, t, tw, bar);
+template <typename R, int N, int P, bool INV, int SSTR, int G>
+__device__ __forceinline__ void fft(C2<R> (&v)[Plan<N, P>::E], C2<R>* sb, int t, const C2<R>* tw, int bar) {
+    stage<R, N, P, 0, INV, SSTR, G>(v, sb, t, tw, bar);
+    if constexpr (Plan<N, P>::L > 1) stage<R, N, P, 1, INV, SSTR, G>(v, sb, t, tw, bar);
+    if constexpr (Plan<N, P>::L > 2) stage<R, N, P, 2, INV, SSTR, G>(v, sb, t, tw, bar);
 }
 
 }  // namespace gpe

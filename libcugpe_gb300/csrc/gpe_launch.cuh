@@ -11,26 +11,26 @@ namespace gpe {
 // Threads per CTA: 128, or one pencil group of the wanted column width when
 // a group is larger (x and y pencils of 256 and 512 points in the FP32 form).
 // A lattice with fewer pencils than a CTA holds runs a partial last CTA.
-template <typename R, int N, int AX> constexpr int pass_nt() {
+template <typename R, int N, int AX, int P = 0> constexpr int pass_nt() {
     if constexpr (AX == AX_Z) {
         return 128;
     } else {
-        constexpr int T = N / Plan<N>::E;
+        constexpr int T = N / Plan<N, P>::E;
         constexpr int want = ((32 / T) > cw_target<R, N, AX>()) ? (32 / T) : cw_target<R, N, AX>();
         return (T * want > 128) ? T * want : 128;
     }
 }
 
-template <typename R, int N, int AX, int NT, int CLS>
+template <typename R, int N, int AX, int NT, int CLS, int P>
 cudaError_t launch_one(const PassArgs<R>& a, size_t pencils, cudaStream_t st) {
-    using Geo = PassGeom<R, N, AX, NT>;
+    using Geo = PassGeom<R, N, AX, NT, P>;
     static bool configured = false;  // per instantiation, single device
     if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(pass_kernel<R, N, AX, NT, CLS>,
+        cudaError_t e = cudaFuncSetAttribute(pass_kernel<R, N, AX, NT, CLS, P>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Geo::SMEM_MAX);
         if (e != cudaSuccess) return e;
         // the passes use shared memory, not L1, for reuse: ask for the largest carveout
-        e = cudaFuncSetAttribute(pass_kernel<R, N, AX, NT, CLS>, cudaFuncAttributePreferredSharedMemoryCarveout,
+        e = cudaFuncSetAttribute(pass_kernel<R, N, AX, NT, CLS, P>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  (int)cudaSharedmemCarveoutMaxShared);
         if (e != cudaSuccess) return e;
         configured = true;
@@ -46,7 +46,7 @@ cudaError_t launch_one(const PassArgs<R>& a, size_t pencils, cudaStream_t st) {
             cudaError_t e = cudaGetDevice(&dev);
             if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
             if (e == cudaSuccess)
-                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pass_kernel<R, N, AX, NT, CLS>, NT, smem);
+                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pass_kernel<R, N, AX, NT, CLS, P>, NT, smem);
             if (e != cudaSuccess) return e;
             resident = (unsigned)((per_sm > 0 ? per_sm : 1) * sms);
         }
@@ -67,13 +67,13 @@ cudaError_t launch_one(const PassArgs<R>& a, size_t pencils, cudaStream_t st) {
     // programmatic dependent launch: +2% steps/s for the FP32 form (128^3-512^3); the FP64 passes
     // ran slower with it (64^3: 4230 against 4679 steps/s), so they launch in plain stream order
     cfg.numAttrs = (sizeof(R) == 4) ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, pass_kernel<R, N, AX, NT, CLS>, b);
+    return cudaLaunchKernelEx(&cfg, pass_kernel<R, N, AX, NT, CLS, P>, b);
 }
 
-template <typename R, int N, int AX>
+template <typename R, int N, int AX, int P>
 cudaError_t launch_ax(const PassArgs<R>& a, size_t pencils, cudaStream_t st, unsigned* grid_out) {
-    constexpr int NT = pass_nt<R, N, AX>();
-    *grid_out = (unsigned)((pencils + PassGeom<R, N, AX, NT>::W - 1) / PassGeom<R, N, AX, NT>::W);
+    constexpr int NT = pass_nt<R, N, AX, P>();
+    *grid_out = (unsigned)((pencils + PassGeom<R, N, AX, NT, P>::W - 1) / PassGeom<R, N, AX, NT, P>::W);
     switch (op_class(a.pre, a.mid, a.post, a.flags)) {
         case C_KIN:
             // FP32 x pencils of 512 points: the persistent pass overlaps loads and transforms (measured
@@ -81,57 +81,75 @@ cudaError_t launch_ax(const PassArgs<R>& a, size_t pencils, cudaStream_t st, uns
             if constexpr (sizeof(R) == 4 && N >= 512 && AX == AX_X) {
                 if ((a.flags & ~(F_VEXTRA | F_DIRECT)) == (F_KIN | F_STORE) && a.pre == PRE_NONE &&
                     a.mid == MID_NONE && a.post == POST_NONE)
-                    return launch_one<R, N, AX, NT, C_KINP>(a, pencils, st);
+                    return launch_one<R, N, AX, NT, C_KINP, P>(a, pencils, st);
             }
-            return launch_one<R, N, AX, NT, C_KIN>(a, pencils, st);
-        case C_EPI: return launch_one<R, N, AX, NT, C_EPI>(a, pencils, st);
-        case C_LAP: return launch_one<R, N, AX, NT, C_LAP>(a, pencils, st);
-        case C_DIP: return launch_one<R, N, AX, NT, C_DIP>(a, pencils, st);
+            return launch_one<R, N, AX, NT, C_KIN, P>(a, pencils, st);
+        case C_EPI: return launch_one<R, N, AX, NT, C_EPI, P>(a, pencils, st);
+        case C_LAP: return launch_one<R, N, AX, NT, C_LAP, P>(a, pencils, st);
+        case C_DIP: return launch_one<R, N, AX, NT, C_DIP, P>(a, pencils, st);
         case C_EPI_D:
-            if constexpr (sizeof(R) == 4 && N <= 128) return launch_one<R, N, AX, NT, C_EPI_D>(a, pencils, st);
+            if constexpr (sizeof(R) == 4 && N <= 128) return launch_one<R, N, AX, NT, C_EPI_D, P>(a, pencils, st);
             else return cudaErrorInvalidValue;
         case C_LAP_D:
-            if constexpr (sizeof(R) == 4 && N <= 128) return launch_one<R, N, AX, NT, C_LAP_D>(a, pencils, st);
+            if constexpr (sizeof(R) == 4 && N <= 128) return launch_one<R, N, AX, NT, C_LAP_D, P>(a, pencils, st);
             else return cudaErrorInvalidValue;
-        default: return launch_one<R, N, AX, NT, C_EN>(a, pencils, st);
+        default: return launch_one<R, N, AX, NT, C_EN, P>(a, pencils, st);
     }
 }
 
-template <typename R, int N>
+template <typename R, int N, int P>
 cudaError_t launch_n(const PassArgs<R>& a, int axis, size_t pencils, cudaStream_t st, unsigned* g);
 
 #ifdef GPE_PASS_DEFINITIONS
-template <typename R, int N>
+template <typename R, int N, int P>
 cudaError_t launch_n(const PassArgs<R>& a, int axis, size_t pencils, cudaStream_t st, unsigned* g) {
     switch (axis) {
-        case AX_X: return launch_ax<R, N, AX_X>(a, pencils, st, g);
-        case AX_Y: return launch_ax<R, N, AX_Y>(a, pencils, st, g);
-        default: return launch_ax<R, N, AX_Z>(a, pencils, st, g);
+        case AX_X: return launch_ax<R, N, AX_X, P>(a, pencils, st, g);
+        case AX_Y: return launch_ax<R, N, AX_Y, P>(a, pencils, st, g);
+        default: return launch_ax<R, N, AX_Z, P>(a, pencils, st, g);
     }
 }
 #endif
 
+// Radix plan a pass over pencils of n points runs with when `plan` is requested: the alternative
+// plans exist for FP32 pencils of 32 to 512 points; everything else runs plan 0.
+inline int effective_plan(int plan, int n, bool fp32) { return (plan == 1 && fp32 && has_plan1(n)) ? 1 : 0; }
+
 // Upper bound on the CTAs of a pass over `pencils` pencils (sizes the partials buffer).
 inline size_t pass_grid_bound(size_t pencils) { return pencils; }
 
+// Launches one pass with the radix plan `a.plan` (whose twiddles `a.tw` holds).
 template <typename R>
 cudaError_t launch_pass(const PassArgs<R>& a, int N, int axis, size_t pencils, cudaStream_t st) {
     unsigned g = 0;
+    if (a.plan != effective_plan(a.plan, N, sizeof(R) == 4)) return cudaErrorInvalidValue;
+    if constexpr (sizeof(R) == 4) {
+        if (a.plan == 1) {
+            switch (N) {
+                case 32: return launch_n<R, 32, 1>(a, axis, pencils, st, &g);
+                case 64: return launch_n<R, 64, 1>(a, axis, pencils, st, &g);
+                case 128: return launch_n<R, 128, 1>(a, axis, pencils, st, &g);
+                case 256: return launch_n<R, 256, 1>(a, axis, pencils, st, &g);
+                case 512: return launch_n<R, 512, 1>(a, axis, pencils, st, &g);
+                default: return cudaErrorInvalidValue;
+            }
+        }
+    }
     switch (N) {
-        case 8: return launch_n<R, 8>(a, axis, pencils, st, &g);
-        case 16: return launch_n<R, 16>(a, axis, pencils, st, &g);
-        case 32: return launch_n<R, 32>(a, axis, pencils, st, &g);
-        case 64: return launch_n<R, 64>(a, axis, pencils, st, &g);
-        case 128: return launch_n<R, 128>(a, axis, pencils, st, &g);
-        case 256: return launch_n<R, 256>(a, axis, pencils, st, &g);
-        case 512: return launch_n<R, 512>(a, axis, pencils, st, &g);
+        case 8: return launch_n<R, 8, 0>(a, axis, pencils, st, &g);
+        case 16: return launch_n<R, 16, 0>(a, axis, pencils, st, &g);
+        case 32: return launch_n<R, 32, 0>(a, axis, pencils, st, &g);
+        case 64: return launch_n<R, 64, 0>(a, axis, pencils, st, &g);
+        case 128: return launch_n<R, 128, 0>(a, axis, pencils, st, &g);
+        case 256: return launch_n<R, 256, 0>(a, axis, pencils, st, &g);
+        case 512: return launch_n<R, 512, 0>(a, axis, pencils, st, &g);
         default: return cudaErrorInvalidValue;
     }
 }
 
 }  // namespace gpe
 
-// One translation unit per (precision, pencil length) instantiates
-// launch_n<R, N>; launch_pass<R> switches over them.
-#define GPE_INSTANTIATE_N(R, N) \
-    template cudaError_t gpe::launch_n<R, N>(const gpe::PassArgs<R>&, int, size_t, cudaStream_t, unsigned*);
+// One translation unit per (precision, pencil length, radix plan) instantiates
+// launch_n<R, N, P>; launch_pass<R> switches over them.
+#define GPE_INSTANTIATE_N(R, N, P) \
+    template cudaError_t gpe::launch_n<R, N, P>(const gpe::PassArgs<R>&, int, size_t, cudaStream_t, unsigned*);

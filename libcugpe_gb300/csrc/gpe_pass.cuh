@@ -111,7 +111,8 @@ struct PassArgs {
     int vsteps, vslices;
     const C2<R>* ktab;   // kinetic factors of this axis, incl. 1/N_a
     const R* ltab;       // Laplacian / kinetic-energy weights of this axis
-    const C2<R>* tw;     // exp(-2 pi i p / N_a)
+    const C2<R>* tw;     // stage twiddles of this axis's radix plan
+    int plan;            // radix plan of this axis (Plan<N, plan>), matching tw
     DynState* dyn;
     double* partials;    // [gridDim.x][NRED]
     int lx, ly, lz;      // log2 of the lattice sides
@@ -312,8 +313,8 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 template <typename R, int N, int AX> __host__ __device__ constexpr int cw_target() {
     return (sizeof(C2<R>) == 16) ? 2 : (AX == AX_X) ? 16 : 8;
 }
-template <typename R, int N, int AX, int NT> __host__ __device__ constexpr int pass_cw() {
-    constexpr int T = N / Plan<N>::E;
+template <typename R, int N, int AX, int NT, int P = 0> __host__ __device__ constexpr int pass_cw() {
+    constexpr int T = N / Plan<N, P>::E;
     constexpr int want = ((32 / T) > cw_target<R, N, AX>()) ? (32 / T) : cw_target<R, N, AX>();
     return (T * want <= NT) ? want : ((NT / T) > 0 ? NT / T : 1);
 }
@@ -323,15 +324,15 @@ template <typename R, int N, int AX, int NT> __host__ __device__ constexpr int p
 //  one pencil spans T/32 warps (T > 32, 512 points).
 //  y/x pencils: a group of G = T*CW threads holds CW adjacent columns, column
 //  fastest, so a warp-wide access covers 32/T rows of CW contiguous points.
-template <typename R, int N, int AX, int NT>
+template <typename R, int N, int AX, int NT, int P = 0>
 struct PassGeom {
-    static constexpr int E = Plan<N>::E;
+    static constexpr int E = Plan<N, P>::E;
     static constexpr int T = N / E;
-    static constexpr int CW = (AX == AX_Z) ? ((32 / T) > 0 ? 32 / T : 1) : pass_cw<R, N, AX, NT>();
+    static constexpr int CW = (AX == AX_Z) ? ((32 / T) > 0 ? 32 / T : 1) : pass_cw<R, N, AX, NT, P>();
     static constexpr int G = (AX == AX_Z) ? (T > 32 ? T : 32) : T * CW;
     static constexpr int W = NT / T;  // pencils per CTA
     static constexpr int ROW = padded_len<N>();
-    static constexpr int TW = tw_len<N>();
+    static constexpr int TW = tw_len<N, P>();
     static constexpr size_t TAB_BYTES = (((size_t)(TW + N) * sizeof(C2<R>) + N * sizeof(R)) + 15) & ~(size_t)15;
     static constexpr size_t EXCH_BYTES = (size_t)W * ROW * sizeof(C2<R>);
     static constexpr size_t SMEM_BASE = TAB_BYTES + EXCH_BYTES;
@@ -344,9 +345,11 @@ struct PassGeom {
     // resident threads per SM the register allocation aims for: FP32 pencils up to 128 points fit
     // 7 CTAs of 128 threads in 72 registers without spills, 256-point ones 6 in 80, which runs the
     // 128^3 and 256^3 passes (1-2 waves of CTAs) in fewer rounds (measured: +8% RTE, +20% ITE
-    // steps/s at 128^3, +2% / +16% at 256^3); 512-point pencils, at 8 points per thread, fit
-    // 1024 threads in 64 registers without spills
-    static constexpr int THREADS_SM = (sizeof(R) == 4) ? (N <= 128 ? 896 : N <= 256 ? 768 : 1024) : 256;
+    // steps/s at 128^3, +2% / +16% at 256^3); pencils of 128 to 512 points at 8 points per thread
+    // fit 1024 threads in 64 registers without spills (512 points: +16% steps/s at 512^3 against 16
+    // points per thread in 512 threads)
+    static constexpr int THREADS_SM = (sizeof(R) == 4)
+        ? (E == 8 ? (N <= 64 ? 896 : 1024) : (N <= 128 ? 896 : N <= 256 ? 768 : 512)) : 256;
     static constexpr int MINB = (THREADS_SM / NT) > 0 ? THREADS_SM / NT : 1;
     static_assert(NT % G == 0 && NT % 32 == 0, "threads per CTA must hold whole groups");
     static_assert(SMEM_BASE + 2 * (size_t)E * NT * sizeof(C2<R>) <= SMEM_CAP,
@@ -373,11 +376,11 @@ __host__ __device__ inline int op_class(int pre, int mid, int post, uint32_t fla
 
 // The pass over the pencils of one lattice, as CTA `blk` of `nblk` CTAs
 // working on it (a standalone launch, or one condensate of a batch).
-template <typename R, int N, int AX, int NT, int CLS>
+template <typename R, int N, int AX, int NT, int CLS, int P = 0>
 __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, uint32_t nblk) {
     constexpr bool DIRECT = (CLS == C_EPI_D || CLS == C_LAP_D);
     constexpr int K = (CLS == C_EPI_D) ? C_EPI : (CLS == C_LAP_D) ? C_LAP : CLS;  // base class
-    using Geo = PassGeom<R, N, AX, NT>;
+    using Geo = PassGeom<R, N, AX, NT, P>;
     constexpr int E = Geo::E, T = Geo::T, CW = Geo::CW, G = Geo::G, W = Geo::W, ROW = Geo::ROW;
     constexpr int SSTR = (AX == AX_Z) ? 1 : CW;
     constexpr bool FIN = (K == C_EPI || K == C_EN || K == C_DIP);
@@ -522,13 +525,13 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     // the pending norm factor, as they were taken from the unscaled psi), 2 adds
     // them into slots C/D for the MID op.  x is psi again afterwards.
     auto wz_grad = [&](int mode) {
-        fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
+        fft<R, N, P, false, SSTR, G>(x, sb, t, stw, bar);
 #pragma unroll
         for (int q = 0; q < E; q++) {
             const R k = __ldg(a.ld1 + t + T * q);
             x[q] = mk<R>(-k * x[q].y, k * x[q].x);
         }
-        fft<R, N, true, SSTR, G>(x, sb, t, stw, bar);
+        fft<R, N, P, true, SSTR, G>(x, sb, t, stw, bar);
         cp_async_wait_all();
         if (valid) {
             const R f2 = scale_in ? s_prev * s_prev : (R)1;
@@ -602,7 +605,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
 #pragma unroll
             for (int q = 0; q < E; q++) x[q] = mk<R>(density(a.ph, x[q]), (R)0);
         }
-        if (dm == DIP_DENS_FWD || dm == DIP_FWD || dm == DIP_VDD) fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
+        if (dm == DIP_DENS_FWD || dm == DIP_FWD || dm == DIP_VDD) fft<R, N, P, false, SSTR, G>(x, sb, t, stw, bar);
         if (dm == DIP_VDD) {
 #pragma unroll
             for (int q = 0; q < E; q++) {
@@ -611,7 +614,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                 x[q] = cscale(x[q], vdd_k(a, ix, iy, iz));
             }
         }
-        if (dm != DIP_DENS_FWD && dm != DIP_FWD) fft<R, N, true, SSTR, G>(x, sb, t, stw, bar);
+        if (dm != DIP_DENS_FWD && dm != DIP_FWD) fft<R, N, P, true, SSTR, G>(x, sb, t, stw, bar);
         if (dm == DIP_STEP || dm == DIP_EN) {
             cp_async_wait_all();
             if (valid) {
@@ -637,10 +640,10 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                 from_cells();
             }
             if (dm == DIP_STEP && (a.flags & F_KIN)) {
-                fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
+                fft<R, N, P, false, SSTR, G>(x, sb, t, stw, bar);
 #pragma unroll
                 for (int q = 0; q < E; q++) x[q] = cmul(x[q], skt[t + T * q]);
-                fft<R, N, true, SSTR, G>(x, sb, t, stw, bar);
+                fft<R, N, P, true, SSTR, G>(x, sb, t, stw, bar);
             }
             if (a.flags & F_REDUCE) {
                 if constexpr (sizeof(R) == 4) {
@@ -657,7 +660,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
 
     // ------------------------------------------------- energy: forward only
     if constexpr (K == C_EN) {
-        fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
+        fft<R, N, P, false, SSTR, G>(x, sb, t, stw, bar);
 #pragma unroll
         for (int q = 0; q < E; q++) {
             const double w = (double)slt[t + T * q];
@@ -672,10 +675,10 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
             for (int q = 0; q < E; q++) slotB[q * NT + tid] = x[q];
         }
         if (a.flags & F_WZ) wz_grad(a.mid == MID_LAP_STORE ? 0 : a.mid == MID_LAP_ACC ? 1 : 2);
-        fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
+        fft<R, N, P, false, SSTR, G>(x, sb, t, stw, bar);
 #pragma unroll
         for (int q = 0; q < E; q++) x[q] = cscale(x[q], slt[t + T * q]);
-        fft<R, N, true, SSTR, G>(x, sb, t, stw, bar);
+        fft<R, N, P, true, SSTR, G>(x, sb, t, stw, bar);
         cp_async_wait_all();
         if (valid) {
             if (a.mid == MID_LAP_STORE) {
@@ -728,10 +731,10 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     // ---------------------------------------------------------- kinetic pair
     if constexpr (K != C_EN && K != C_DIP) {  // the dipolar passes run their own transforms
         if (K != C_LAP || (a.flags & F_KIN)) {
-            fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
+            fft<R, N, P, false, SSTR, G>(x, sb, t, stw, bar);
 #pragma unroll
             for (int q = 0; q < E; q++) x[q] = cmul(x[q], skt[t + T * q]);
-            fft<R, N, true, SSTR, G>(x, sb, t, stw, bar);
+            fft<R, N, P, true, SSTR, G>(x, sb, t, stw, bar);
         }
     }
 
@@ -795,10 +798,10 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                 for (int q = 0; q < E; q++) slotB[q * NT + tid] = x[q];
                 wz_grad(0);
             }
-            fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
+            fft<R, N, P, false, SSTR, G>(x, sb, t, stw, bar);
 #pragma unroll
             for (int q = 0; q < E; q++) x[q] = cscale(x[q], slt[t + T * q]);
-            fft<R, N, true, SSTR, G>(x, sb, t, stw, bar);
+            fft<R, N, P, true, SSTR, G>(x, sb, t, stw, bar);
             if (valid) {
 #pragma unroll
                 for (int q = 0; q < E; q++) a.lap[at(q)] = x[q];
@@ -841,9 +844,9 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
 // walks tiles of W pencils grid-stride, and while it transforms one tile the next tile's points are
 // already on their way into shared memory (cp.async into a staging buffer that only the copying
 // thread reads back), so the loads of one tile overlap the arithmetic of the previous one.
-template <typename R, int N, int AX, int NT>
+template <typename R, int N, int AX, int NT, int P>
 __device__ __forceinline__ void kin_pipe_body(const PassArgs<R>& a) {
-    using Geo = PassGeom<R, N, AX, NT>;
+    using Geo = PassGeom<R, N, AX, NT, P>;
     constexpr int E = Geo::E, T = Geo::T, CW = Geo::CW, G = Geo::G, W = Geo::W, ROW = Geo::ROW;
     constexpr int SSTR = (AX == AX_Z) ? 1 : CW;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -904,10 +907,10 @@ __device__ __forceinline__ void kin_pipe_body(const PassArgs<R>& a) {
 #pragma unroll
         for (int q = 0; q < E; q++) x[q] = valid ? stg[q * NT + tid] : mk<R>((R)0, (R)0);
         if (tile + gridDim.x < ntiles) prefetch(tile + gridDim.x);
-        fft<R, N, false, SSTR, G>(x, sb, t, stw, bar);
+        fft<R, N, P, false, SSTR, G>(x, sb, t, stw, bar);
 #pragma unroll
         for (int q = 0; q < E; q++) x[q] = cmul(x[q], skt[t + T * q]);
-        fft<R, N, true, SSTR, G>(x, sb, t, stw, bar);
+        fft<R, N, P, true, SSTR, G>(x, sb, t, stw, bar);
         if (valid) {
 #pragma unroll
             for (int q = 0; q < E; q++) a.out[tb + ((uint32_t)(T * q) << lstr)] = x[q];
@@ -916,11 +919,11 @@ __device__ __forceinline__ void kin_pipe_body(const PassArgs<R>& a) {
     cp_async_wait_all();
 }
 
-template <typename R, int N, int AX, int NT, int CLS>
-__global__ void __launch_bounds__(NT, PassGeom<R, N, AX, NT>::MINB)
+template <typename R, int N, int AX, int NT, int CLS, int P>
+__global__ void __launch_bounds__(NT, PassGeom<R, N, AX, NT, P>::MINB)
 pass_kernel(const PassArgs<R> a) {
-    if constexpr (CLS == C_KINP) kin_pipe_body<R, N, AX, NT>(a);
-    else pass_body<R, N, AX, NT, CLS>(a, blockIdx.x, gridDim.x);
+    if constexpr (CLS == C_KINP) kin_pipe_body<R, N, AX, NT, P>(a);
+    else pass_body<R, N, AX, NT, CLS, P>(a, blockIdx.x, gridDim.x);
 }
 
 }  // namespace gpe

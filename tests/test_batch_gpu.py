@@ -64,6 +64,26 @@ def test_batch_against_fp64_oracle_and_inactive(cuda_device, gpe_lib):
         assert rel(b.engines[i].get_psi()[1], o.get_psi()[1]) <= 2e-5 * 10
 
 
+def test_batch_radix_plan_1_against_fp64_oracle(cuda_device, gpe_lib):
+    """The batched launches under the alternative radix plan (every condensate's pencils at the other
+    point count per thread) against the FP64 oracle."""
+    shapes = [(32, 32, 32), (64, 32, 32), (128, 32, 32), (32, 256, 32)]
+    b = g.Batch(shapes, interactions=-1, alpha=0.0, beta=1.0, dt=0.05)
+    b.set_fft_plan(1)
+    psis = []
+    for i, s in enumerate(shapes):
+        psis.append(configs.random_state(s, seed=60 + i))
+        b.engines[i].set_user_params(params_for(i))
+        b.engines[i].set_psi(0.0, psis[i])
+    b.evolve(10)
+    for i, s in enumerate(shapes):
+        o = oracle.Oracle(s, -1, 0.0, 1.0, 0.05, 1.0, threads=4)
+        o.set_user_params(params_for(i))
+        o.set_psi(0.0, psis[i])
+        o.evolve_qf(10)
+        assert rel(b.engines[i].get_psi()[1], o.get_psi()[1]) <= 2e-5 * 10, i
+
+
 def test_batch_rejects_unsupported(cuda_device, gpe_lib):
     with pytest.raises(g.GPEError):
         g.Batch([(16, 16, 16)], precision=g.FP32)
@@ -81,7 +101,8 @@ def test_batch_autotune_keeps_results(cuda_device, gpe_lib):
         return b
     b1, b2 = make(), make()
     choice = b1.autotune(8)
-    assert choice["order"] in (0, 1) and choice["graph_steps"] in (8, 16, 32)
+    assert choice["order"] in (0, 1) and choice["graph_steps"] in (8, 16, 32) and choice["fft_plan"] in (0, 1)
+    b2.set_fft_plan(choice["fft_plan"])  # item order and graph length leave the bits unchanged
     b1.evolve(21)
     b2.evolve(21)
     for i in range(len(SHAPES)):

@@ -358,8 +358,11 @@ def test_autotune_restores_state_and_keeps_results(cuda_device, gpe_lib, precisi
     choice = e.autotune(8)
     assert choice["graph_steps"] in (8, 16, 32) and choice["ms_per_step"] > 0
     assert choice["direct"] in ((0, 1) if precision == g.FP32 else (-1,))
+    assert choice["fft_plan"] in ((0, 1) if precision == g.FP32 else (0,))
+    assert e.get_fft_plan() == choice["fft_plan"]
     after = e.get_psi()
     assert after[0] == before[0] and np.array_equal(after[1], before[1])
+    ref.set_fft_plan(choice["fft_plan"])  # operand mode and graph length leave the bits unchanged
     e.evolve_qf(20)
     ref.evolve_qf(20)
     assert np.array_equal(e.get_psi()[1], ref.get_psi()[1])
@@ -375,6 +378,34 @@ def test_weizsacker_energy_matches_oracle(cuda_device, gpe_lib, precision):
     tol = 1e-10 if precision == g.FP64 else 2e-5
     for a, b in zip(e.energy()[1:], o.energy()[1:]):
         assert abs(a - b) <= tol * max(1.0, abs(b)), (a, b)
+
+
+@pytest.mark.parametrize("shape", [(32, 64, 128), (256, 16, 8), (8, 16, 512), (512, 32, 8)])
+def test_fp32_radix_plan_1_against_oracle(cuda_device, gpe_lib, shape):
+    """The alternative radix plans of FP32 pencils of 32 to 512 points (8 <-> 16 points per thread)
+    against the FP64 oracle, plain and friction schedules, ITE and RTE; plans 0 and 1 agree to FP32
+    rounding."""
+    for case in ("bec_ite", "ufg_rte_qf", "ufg_ite_qf"):
+        e, o, _ = make_pair(shape, case, precision=g.FP32)
+        e0, _, _ = make_pair(shape, case, precision=g.FP32)
+        e.set_fft_plan(1)
+        assert e.get_fft_plan() == 1 and e0.get_fft_plan() == 0
+        e.evolve_qf(2)
+        o.evolve_qf(2)
+        e0.evolve_qf(2)
+        p1, p0, po = e.get_psi()[1], e0.get_psi()[1], o.get_psi()[1]
+        assert rel(p1, po) <= 2 * TOL_FP32_STEP, (case, rel(p1, po))
+        assert rel(p1, p0) <= 2 * TOL_FP32_STEP, (case, rel(p1, p0))
+        for a, b in zip(e.energy()[1:], o.energy()[1:]):
+            assert abs(a - b) <= 1e-5 * max(1.0, abs(b)), (case, a, b)
+
+
+def test_fp64_rejects_radix_plan_1(cuda_device, gpe_lib):
+    e, _, _ = make_pair((16, 16, 32), "bec_ite")
+    with pytest.raises(g.GPEError):
+        e.set_fft_plan(1)
+    e.set_fft_plan(0)
+    assert e.get_fft_plan() == 0
 
 
 @pytest.mark.parametrize("shape", [(16, 256, 16), (512, 16, 8), (8, 8, 512), (256, 256, 16)])
