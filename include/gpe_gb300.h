@@ -233,6 +233,8 @@ int gpe_gb_energy_dipolar(gpe_gb_engine* e, double* t, double* edip);
  * (plan 1 on an FP64 engine: GPE_ERR_ARGUMENT).  Both plans compute the same
  * transform; results differ only by FP32 rounding. */
 int gpe_gb_set_fft_plan(gpe_gb_engine* e, int plan);
+/* *plan: 0, 1, or 2 when the autotuner chose a plan per fused pass
+ * (gpe_gb_set_fft_plan clears that choice). */
 int gpe_gb_get_fft_plan(const gpe_gb_engine* e, int* plan);
 /* Plan of every condensate's passes in a batch (one plan per launch). */
 int gpe_gb_batch_set_fft_plan(gpe_gb_batch* b, int plan);
@@ -241,8 +243,11 @@ int gpe_gb_batch_set_fft_plan(gpe_gb_batch* b, int plan);
  * (FP32), pass operands staged in shared memory or read where used (FP32,
  * pencils <= 128 points), and 8, 16 or 32 steps per replayed CUDA graph --
  * keeps the fastest, and puts psi, time and step counter back as they were.
- * Outputs (may be NULL): the chosen operand mode (-1 when there is no
- * choice), graph steps, radix plan, ms per step. */
+ * With both radix plans timed, each fused pass of the steady schedule then
+ * gets the plan under which it ran faster (CUDA events around every pass),
+ * kept if the whole step is faster.  Outputs (may be NULL): the chosen
+ * operand mode (-1 when there is no choice), graph steps, radix plan (0, 1,
+ * or 2 for a plan per fused pass), ms per step. */
 int gpe_gb_autotune(gpe_gb_engine* e, int nsteps, int* direct, int* graph_steps, int* fft_plan,
                     double* ms_per_step);
 /* The same for a batch: radix plan, item order within each launch (0 as

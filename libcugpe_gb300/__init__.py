@@ -259,7 +259,8 @@ class Engine:
 
     def autotune(self, nsteps=32):
         """Times each launch configuration on this engine's state and keeps the fastest; psi, time
-        and step counter are restored.  Returns {"direct", "graph_steps", "fft_plan", "ms_per_step"}."""
+        and step counter are restored.  Returns {"direct", "graph_steps", "fft_plan", "ms_per_step"};
+        fft_plan 2 means a radix plan chosen per fused pass."""
         d, c, p, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
         _check(_lib().gpe_gb_autotune(self._h, int(nsteps), ctypes.byref(d), ctypes.byref(c), ctypes.byref(p),
                                       ctypes.byref(ms)), "autotune")

@@ -231,6 +231,9 @@ struct Engine {
     int direct_mode = -1;   // operands read where used: -1 by lattice size, 0 staged, 1 direct (autotuner)
     int graph_chunk = 16;   // steps per replayed graph (autotuner)
     int fft_plan = 0;       // radix plan of the pencil FFTs: 0 default, 1 alternative (FP32; autotuner)
+    // radix plan per fused pass of the steady schedule, chosen by the autotuner from per-pass timings
+    // (key: pass_key); passes without an entry run fft_plan
+    std::vector<std::pair<uint64_t, int>> pass_plan;
     bool graph_dirty = true;
     unsigned version = 0;  // bumped whenever tables or captured arguments change
     bool lap_valid = false;  // lap holds the z-Laplacian term of the current psi
@@ -406,6 +409,12 @@ struct PassDesc {
 };
 enum { B_NONE = 0, B_PSI = 1, B_PSI2 = 2 };
 
+// Identifies a fused pass by what it computes (axis, ops, flags), not by its buffers.
+static uint64_t pass_key(const PassDesc& d) {
+    return ((uint64_t)d.flags << 32) | ((uint64_t)(d.axis & 3) << 24) | ((uint64_t)(d.pre & 0xff) << 16) |
+           ((uint64_t)(d.mid & 0xff) << 8) | (uint64_t)(d.post & 0xff);
+}
+
 // The reference step sequence (dev/gpe_engine.cu:1035-1106) as fused passes.
 static std::vector<PassDesc> schedule(const Engine* e, bool first) {
     std::vector<PassDesc> s;
@@ -504,6 +513,14 @@ template <typename R>
 static PassArgs<R> desc_args(const Engine* e, const PassDesc& d) {
     PassArgs<R> a = base_args<R>(e);
     axis_args(e, a, d.axis);
+    if (!e->pass_plan.empty()) {
+        const uint64_t k = pass_key(d);
+        for (const auto& pp : e->pass_plan)
+            if (pp.first == k) {
+                a.plan = effective_plan(pp.second, e->n3[d.axis], e->prec == GPE_PRECISION_FP32);
+                a.tw = (const C2<R>*)e->ax[d.axis].tw[a.plan];
+            }
+    }
     a.ltab = (const R*)e->ax[d.axis].lqf;
     a.in = (const C2<R>*)(d.in == B_PSI ? e->psi : e->psi2);
     a.out = (C2<R>*)(d.out == B_PSI ? e->psi : d.out == B_PSI2 ? e->psi2 : nullptr);
@@ -2048,8 +2065,9 @@ int gpe_gb_set_fft_plan(gpe_gb_engine* h, int plan) {
     Engine* e = &h->e;
     if (plan != 0 && plan != 1) return GPE_ERR_ARGUMENT;
     if (plan == 1 && e->prec != GPE_PRECISION_FP32) return GPE_ERR_ARGUMENT;
-    if (plan != e->fft_plan) {
+    if (plan != e->fft_plan || !e->pass_plan.empty()) {
         e->fft_plan = plan;
+        e->pass_plan.clear();
         gpe::drop_graph(e);
         e->graph_dirty = true;
         e->version++;  // batches holding this engine rebuild their launches
@@ -2060,7 +2078,7 @@ int gpe_gb_set_fft_plan(gpe_gb_engine* h, int plan) {
 int gpe_gb_get_fft_plan(const gpe_gb_engine* h, int* plan) {
     if (!h) return GPE_ERR_NO_ENGINE;
     if (!plan) return GPE_ERR_ARGUMENT;
-    *plan = h->e.fft_plan;
+    *plan = h->e.pass_plan.empty() ? h->e.fft_plan : 2;
     return 0;
 }
 
@@ -2102,8 +2120,64 @@ int gpe_gb_autotune(gpe_gb_engine* h, int nsteps, int* direct, int* chunk, int* 
             }
         }
     }
+    // per-pass refinement: each fused pass of the steady schedule runs the plan under which it
+    // timed faster (CUDA events around every pass, both plans), kept if the whole step is faster
+    if (!rc && np == 2) {
+        e->direct_mode = (nd == 2) ? bd : -1;
+        e->graph_chunk = bc;
+        const std::vector<gpe::PassDesc> s = gpe::schedule(e, false);
+        const int cap = 32;
+        std::vector<double> t[2];
+        for (int p = 0; p < 2 && !rc; p++) {
+            float ms[cap];
+            double by[cap];
+            int ax[cap], cl[cap], npass = 0;
+            e->fft_plan = p;
+            e->pass_plan.clear();
+            if ((rc = gpe::snap_load(e, &snap))) break;
+            if ((rc = gpe::profile_passes(e, nsteps, ms, by, ax, cl, cap, &npass))) break;
+            if (npass != (int)s.size() || npass > cap) { rc = GPE_ERR_ARGUMENT; break; }
+            t[p].assign(ms, ms + npass);
+        }
+        if (!rc) {
+            std::vector<std::pair<uint64_t, double>> gain;  // per key: time under plan 0 - under plan 1
+            for (size_t i = 0; i < s.size(); i++) {
+                const uint64_t k = gpe::pass_key(s[i]);
+                auto it = std::find_if(gain.begin(), gain.end(), [&](const std::pair<uint64_t, double>& x) {
+                    return x.first == k;
+                });
+                if (it == gain.end()) gain.push_back({k, t[0][i] - t[1][i]});
+                else it->second += t[0][i] - t[1][i];
+            }
+            std::vector<std::pair<uint64_t, int>> plan;
+            bool mixed0 = false, mixed1 = false;
+            for (const auto& x : gain) {
+                plan.push_back({x.first, x.second > 0.0 ? 1 : 0});
+                (x.second > 0.0 ? mixed1 : mixed0) = true;
+            }
+            if (mixed0 && mixed1) {  // a uniform choice was timed above already
+                e->fft_plan = bp;
+                e->pass_plan = plan;
+                gpe::drop_graph(e);
+                e->graph_dirty = true;
+                float ms = 0.f;
+                if (!(rc = gpe::snap_load(e, &snap)) && !(rc = gpe::evolve(e, nsteps, nullptr)) &&
+                    !(rc = gpe::snap_load(e, &snap))) {
+                    cudaEventRecord(a, e->st);
+                    if (!(rc = gpe::evolve(e, nsteps, nullptr))) {
+                        cudaEventRecord(b, e->st);
+                        cudaEventSynchronize(b);
+                        cudaEventElapsedTime(&ms, a, b);
+                    }
+                }
+                if (rc || ms >= best) e->pass_plan.clear();
+                else best = ms;
+            }
+        }
+    }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
+    if (rc) e->pass_plan.clear();
     e->fft_plan = bp;
     e->direct_mode = (nd == 2) ? bd : -1;
     e->graph_chunk = bc;
@@ -2116,7 +2190,7 @@ int gpe_gb_autotune(gpe_gb_engine* h, int nsteps, int* direct, int* chunk, int* 
     if (rc2) return rc2;
     if (direct) *direct = e->direct_mode;
     if (chunk) *chunk = e->graph_chunk;
-    if (fft_plan) *fft_plan = e->fft_plan;
+    if (fft_plan) *fft_plan = e->pass_plan.empty() ? e->fft_plan : 2;
     if (ms_per_step) *ms_per_step = best / nsteps;
     return 0;
 }

@@ -358,14 +358,20 @@ def test_autotune_restores_state_and_keeps_results(cuda_device, gpe_lib, precisi
     choice = e.autotune(8)
     assert choice["graph_steps"] in (8, 16, 32) and choice["ms_per_step"] > 0
     assert choice["direct"] in ((0, 1) if precision == g.FP32 else (-1,))
-    assert choice["fft_plan"] in ((0, 1) if precision == g.FP32 else (0,))
+    assert choice["fft_plan"] in ((0, 1, 2) if precision == g.FP32 else (0,))
     assert e.get_fft_plan() == choice["fft_plan"]
     after = e.get_psi()
     assert after[0] == before[0] and np.array_equal(after[1], before[1])
-    ref.set_fft_plan(choice["fft_plan"])  # operand mode and graph length leave the bits unchanged
+    if choice["fft_plan"] < 2:
+        ref.set_fft_plan(choice["fft_plan"])  # operand mode and graph length leave the bits unchanged
     e.evolve_qf(20)
     ref.evolve_qf(20)
-    assert np.array_equal(e.get_psi()[1], ref.get_psi()[1])
+    if choice["fft_plan"] == 2:  # a plan per fused pass: FP32 rounding of the other factorisations
+        assert rel(e.get_psi()[1], ref.get_psi()[1]) <= 20 * TOL_FP32_STEP
+    else:
+        assert np.array_equal(e.get_psi()[1], ref.get_psi()[1])
+    e.set_fft_plan(0)
+    assert e.get_fft_plan() == 0
 
 
 @pytest.mark.parametrize("precision", [g.FP64, g.FP32])
