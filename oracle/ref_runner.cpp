@@ -26,6 +26,13 @@
 //     Y<k>   gpe_evolve_dipolar(k, &mu) -> "MU mu"
 //     W      gpe_energy_dipolar2() -> "W t edip"  (gpe_energy_dipolar itself indexes -k past the
 //            transform for the k = 0 planes, dev/gpe_engine.cu:1725, and is not called)
+//     Z      gpe_get_psi() then gpe_set_psi(0, psi): restart the clock and step counter on the
+//            current state (the RTE half of the compare harness starts a fresh engine at t = 0)
+//     C<k>/<tol>  ITE loop of test_compare/gpe_imag.c:125-144: gpe_evolve_qf(k), gpe_energy -> "E ...",
+//            until |E_prev - E|/npart < tol (E_prev: the energy printed before)
+//     T<k>/<tmax>  RTE loop of test_compare/gpe_real.c:145-163: gpe_evolve_qf(k), gpe_energy -> "E ...",
+//            until t > tmax
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -58,6 +65,7 @@ int main(int argc, char** argv) {
     CHECK(gpe_set_psi(0.0, psi.data()));
 
     int dump = 0, currents = 0;
+    double etot_last = 0.0;
     size_t pos = 0;
     while (pos < cmds.size()) {
         size_t end = cmds.find(',', pos);
@@ -71,6 +79,24 @@ int main(int argc, char** argv) {
             double t, ek, ei, ee;
             CHECK(gpe_energy(&t, &ek, &ei, &ee));
             printf("E %.17g %.17g %.17g %.17g\n", t, ek, ei, ee);
+            etot_last = ek + ei + ee;
+        } else if (c[0] == 'C' || c[0] == 'T') {
+            int k = 100;
+            double lim = 0.0;
+            sscanf(c.c_str() + 1, "%d/%lf", &k, &lim);
+            for (int iter = 0; iter < 100000; iter++) {
+                double t, ek, ei, ee;
+                CHECK(gpe_evolve_qf(k));
+                CHECK(gpe_energy(&t, &ek, &ei, &ee));
+                printf("E %.17g %.17g %.17g %.17g\n", t, ek, ei, ee);
+                const double et = ek + ei + ee, diff = (etot_last - et) / npart;
+                etot_last = et;
+                if (c[0] == 'C' ? fabs(diff) < lim : t > lim) break;
+            }
+        } else if (c == "Z") {
+            double t;
+            CHECK(gpe_get_psi(&t, psi.data()));
+            CHECK(gpe_set_psi(0.0, psi.data()));
         } else if (c[0] == 'S' || c[0] == 'B') {
             int k = atoi(c.c_str() + 1);
             double mu = 0.0;

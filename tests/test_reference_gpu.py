@@ -111,6 +111,48 @@ def test_bec_64_ite_matches_reference(reference, gpe_lib):
     assert abs(etot - etot_ref) <= 1e-11 * abs(etot_ref)
 
 
+def test_compare_harness_ite_then_rte_matches_reference(reference, gpe_lib):
+    """The reference's own regression harness (test_compare/gpe_imag.c, gpe_real.c, compared by
+    test_compare/compare.py) on its lattice: 256x32x32 UFG, dt = 0.025, npart = 1000, omega = (0.01,
+    0.10, 0.11), psi = 1.  Imaginary time in blocks of 100 steps until the energy per particle changes
+    by < 1e-5 (gpe_imag.c:125-144), then real time from t = 0 to t > 10 (gpe_real.c:145-163).  Same
+    number of blocks, energies after every block and both final states as the reference engine."""
+    shape, dt, npart, params = (256, 32, 32), 0.025, 1000.0, [0.01, 0.10, 0.11, 0.0]
+    build_ref.build([(256, 32, 32, 0)])
+    psi0 = np.ones(shape, dtype=np.complex128)
+    out = ref_run.run(shape, 0, 0.0, 1.0, dt, npart, params, psi0,
+                      ["N", "E", "C100/1e-5", "D", "R", "Z", "E", "T100/10.0", "D"], timeout=1200)
+    e = g.Engine(shape, 0, 0.0, 1.0, dt, npart)
+    e.set_user_params(params)
+    e.set_psi(0.0, psi0)
+    e.normalize_psi()
+    ours = [e.energy()]
+    while True:
+        e.evolve_qf(100)
+        ours.append(e.energy())
+        if abs(sum(ours[-2][1:]) - sum(ours[-1][1:])) / npart < 1e-5:
+            break
+    n_ite = len(ours)
+    _, psi_ite = e.get_psi()
+    e.set_rte_evolution()
+    e.set_psi(0.0, psi_ite)
+    ours.append(e.energy())
+    while True:
+        e.evolve_qf(100)
+        ours.append(e.energy())
+        if ours[-1][0] > 10.0:
+            break
+    _, psi_rte = e.get_psi()
+    ref = out["energy"]
+    assert len(ours) == len(ref), (len(ours), len(ref), n_ite)
+    for a, r in zip(ours, ref):
+        assert a[0] == pytest.approx(r[0], abs=1e-9)
+        for x, y in zip(a[1:], r[1:]):
+            assert abs(x - y) <= 1e-9 * max(1.0, abs(y)), (a, r)
+    assert rel(psi_ite, out["psi"][0]) <= 1e-9
+    assert rel(psi_rte, out["psi"][1]) <= 1e-9
+
+
 @pytest.mark.parametrize("beta", [1.0, 0.0])
 @pytest.mark.parametrize("method", [1, 2, 3, "P"])
 def test_phase_enforcing_evolves_match_reference(reference, gpe_lib, beta, method):
