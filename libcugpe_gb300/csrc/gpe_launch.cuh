@@ -77,7 +77,8 @@ cudaError_t launch_ax(const PassArgs<R>& a, size_t pencils, cudaStream_t st, uns
     switch (op_class(a.pre, a.mid, a.post, a.flags)) {
         case C_KIN:
             // FP32 x pencils of 512 points: the persistent pass overlaps loads and transforms (measured
-            // 923 -> 809 us per pass at 512^3; on y pencils and at 256 points it was slower)
+            // at 512^3 with 16 points per thread: 923 -> 809 us per pass; on y pencils, at either point
+            // count, and at 256 points it was slower)
             if constexpr (sizeof(R) == 4 && N >= 512 && AX == AX_X) {
                 if ((a.flags & ~(F_VEXTRA | F_DIRECT)) == (F_KIN | F_STORE) && a.pre == PRE_NONE &&
                     a.mid == MID_NONE && a.post == POST_NONE)

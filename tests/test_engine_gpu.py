@@ -416,7 +416,7 @@ def test_fp64_rejects_radix_plan_1(cuda_device, gpe_lib):
 
 @pytest.mark.parametrize("shape", [(16, 256, 16), (512, 16, 8), (8, 8, 512), (256, 256, 16)])
 def test_fp32_long_pencils_against_oracle(cuda_device, gpe_lib, shape):
-    """FP32 pencils of 256 and 512 points (persistent kinetic passes with prefetch, 256/512-thread CTAs
+    """FP32 pencils of 256 and 512 points (persistent kinetic passes with prefetch, 256/1024-thread CTAs
     on x) against the FP64 oracle, plain and friction schedules."""
     for case in ("bec_rte", "ufg_rte_qf"):
         e, o, _ = make_pair(shape, case, precision=g.FP32)
