@@ -406,6 +406,38 @@ def test_fp32_radix_plan_1_against_oracle(cuda_device, gpe_lib, shape):
             assert abs(a - b) <= 1e-5 * max(1.0, abs(b)), (case, a, b)
 
 
+@pytest.mark.parametrize("what", ["dipolar", "currents", "weizsacker"])
+def test_fp32_radix_plan_1_other_passes(cuda_device, gpe_lib, what):
+    """The dipolar convolution passes, the current passes and the Weizsaecker sums under the
+    alternative radix plans, against the FP64 oracle with the FP32 tolerances of plan 0."""
+    shape = (32, 64, 128)
+    if what == "dipolar":
+        e, o = make_dip_pair(shape, 1.0, 0.0, precision=g.FP32)
+        e.set_fft_plan(1)
+        e.evolve_dipolar(1)
+        o.evolve_dipolar(1)
+        assert rel(e.get_psi()[1], o.get_psi()[1]) <= TOL_FP32_STEP
+        e.evolve_dipolar(10)
+        o.evolve_dipolar(10)
+        assert rel(e.get_psi()[1], o.get_psi()[1]) <= 10 * TOL_FP32_STEP
+        assert e.energy_dipolar()[1] == pytest.approx(o.energy_dipolar(), rel=1e-5)
+    elif what == "currents":
+        e, o, _ = make_pair(shape, "bec_rte", precision=g.FP32)
+        e.set_fft_plan(1)
+        ref, got = o.get_currents(), e.get_currents()
+        for a in range(1, 4):
+            assert rel(got[a], ref[a]) <= 5e-5, (a, rel(got[a], ref[a]))
+    else:
+        e, o, _ = make_wz_pair(shape, "ufg_rte_qf", precision=g.FP32)
+        e.set_fft_plan(1)
+        e.evolve_qf(1)
+        o.evolve_qf(1)
+        assert rel(e.get_psi()[1], o.get_psi()[1]) <= TOL_FP32_STEP
+        e.evolve_qf(10)
+        o.evolve_qf(10)
+        assert rel(e.get_psi()[1], o.get_psi()[1]) <= 10 * TOL_FP32_STEP
+
+
 def test_fp64_rejects_radix_plan_1(cuda_device, gpe_lib):
     e, _, _ = make_pair((16, 16, 32), "bec_ite")
     with pytest.raises(g.GPEError):
