@@ -93,6 +93,33 @@ def test_ite_noninteracting_ground_state_energy():
     assert abs(mu - 1.5 * w) < 2e-3 * 1.5 * w
 
 
+def test_ite_approaches_the_thomas_fermi_limit_and_lowers_the_energy():
+    """Contact BEC in an isotropic trap at large N a: mu -> mu_TF = (15 N a w^3 / 2^(5/2))^(2/5)
+    (lattice units, hbar = m = 1), from above (the kinetic energy the Thomas-Fermi profile leaves out),
+    closer for the larger N a.  The energy falls through imaginary time down to the splitting error:
+    the fixed point of the split step at finite dt is not the exact minimiser of the lattice energy,
+    so near convergence the energy may rise back by ~1e-10 relative (dt = 0.2)."""
+    n, w = 32, 0.1
+    ratios = []
+    for a in (100.0, 300.0):
+        o = oracle.Oracle((n, n, n), -1, 0.0, 1.0, 0.2, 1.0, threads=4)
+        o.set_user_params([w, w, w, a])
+        o.set_psi(0.0, configs.random_state((n, n, n), seed=2, phase=False))
+        o.normalize_psi()
+        _, ek, ei, ee = o.energy()
+        es, mu = [ek + ei + ee], 0.0
+        for _ in range(20):
+            mu = o.evolve_qf(50)
+            _, ek, ei, ee = o.energy()
+            es.append(ek + ei + ee)
+        assert all(b <= a_ * (1 + 1e-9) for a_, b in zip(es, es[1:]))
+        assert es[-1] < 0.99 * es[0]
+        mu_tf = (15.0 * a * w ** 3 / 2 ** 2.5) ** 0.4
+        ratios.append(mu / mu_tf)
+    assert 1.0 < ratios[1] < ratios[0] < 1.05
+    assert ratios[1] < 1.03
+
+
 def test_rte_conserves_norm_and_energy_without_friction():
     shape = (16, 16, 16)
     o = oracle.Oracle(shape, -1, 1.0, 0.0, 0.02, 1.0, threads=2)
