@@ -46,6 +46,13 @@ def test_argument_checks_without_gpu(gpe_lib):
     assert L.gpe_gb_create(None, 16, 16, 16, -1, 0, 0.0, 1.0, 0.1, 1.0) == g.ERR_ARGUMENT
     assert L.gpe_gb_evolve_qf(None, 1, None) == g.ERR_NO_ENGINE
     assert L.gpe_gb_set_user_params(None, 3, None) == g.ERR_NO_ENGINE
+    # radix plans and autotuners check their handle first
+    p = ctypes.c_int()
+    assert L.gpe_gb_set_fft_plan(None, 1) == g.ERR_NO_ENGINE
+    assert L.gpe_gb_get_fft_plan(None, ctypes.byref(p)) == g.ERR_NO_ENGINE
+    assert L.gpe_gb_batch_set_fft_plan(None, 1) == g.ERR_ARGUMENT
+    assert L.gpe_gb_autotune(None, 8, None, None, None, None) == g.ERR_NO_ENGINE
+    assert L.gpe_gb_batch_autotune(None, 8, None, None, None, None) == g.ERR_ARGUMENT
 
 
 DRIVER = r"""
