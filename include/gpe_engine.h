@@ -17,7 +17,9 @@
  *
  * The reference's other evolution and observable entry points (vortex
  * imprinting, phase enforcing, currents, dipolar evolution and energy) are
- * implemented on the same engine.
+ * implemented on the same engine.  gpe_timing.h (b_t/e_t) and gpe_io.h
+ * (gpe_save_info/gpe_get_info, save_info/get_info) stand in for the
+ * reference's driver-side headers of the same names.
  */
 #ifndef GPE_ENGINE_GB300_DROPIN_H
 #define GPE_ENGINE_GB300_DROPIN_H
@@ -27,6 +29,7 @@
 #include <stdlib.h>
 #include <cuComplex.h>
 #include "gpe_gb300.h"
+#include "gpe_timing.h" /* b_t() / e_t(), as the reference engine header includes its timers */
 
 typedef int gpe_result_t;
 typedef unsigned int uint;

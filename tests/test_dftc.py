@@ -40,6 +40,59 @@ def test_info_reads_a_reference_style_file(tmp_path, gpe_lib):
         dftc.read_info(str(tmp_path / "missing.dftc"))
 
 
+IO_DRIVER = r"""
+#include <cstdio>
+#include <cstring>
+#include "gpe_engine.h"
+#include "gpe_io.h"
+// the driver-side headers of the reference (timers, .dftc.info), as test_vortex/ite_vortex.c and
+// rte_vortex.c use them
+int main(int argc, char** argv) {
+    b_t();
+    char name[256];
+    snprintf(name, sizeof name, "%s/run.dftc", argv[1]);
+    gpe_save_info(name, 64, 32, 16, 0.125, 3, 2.5, 1.5, 0.04, 0.0, 1000.0, 12.5);
+    int nx, ny, nz, nom;
+    double dt, a, ar, w, r0, np, tt = -1.0;
+    gpe_get_info(name, &nx, &ny, &nz, &dt, &nom, &a, &ar, &w, &r0, &np, &tt);
+    printf("NEW %d %d %d %.17g %d %.17g %.17g %.17g %.17g %.17g %.17g\n", nx, ny, nz, dt, nom, a, ar, w, r0, np, tt);
+    snprintf(name, sizeof name, "%s/old.dftc", argv[1]);
+    save_info(name, 8, 16, 32, 0.5, 2, 1.25, 2.0, 0.1, 3.0, 10.0);
+    snprintf(name, sizeof name, "%s/old.dftc.info", argv[1]);
+    get_info(name, &nx, &ny, &nz, &dt, &nom, &a, &ar, &w, &r0, &np);
+    printf("OLD %d %d %d %.17g %d %.17g %.17g %.17g %.17g %.17g\n", nx, ny, nz, dt, nom, a, ar, w, r0, np);
+    const double s = e_t(0);
+    printf("TIME %d %d\n", s >= 0.0 && s < 60.0, e_t(1) == s);
+    return 0;
+}
+"""
+
+
+def test_reference_driver_headers_timing_and_info(tmp_path, gpe_lib):
+    """gpe_timing.h and gpe_io.h: a driver using b_t/e_t, gpe_save_info/gpe_get_info and the older
+    save_info/get_info compiles against include/ and runs without a GPU; the new-style header is the
+    one dftc.read_info parses, for the functional given by -DINTERACTIONS."""
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src, exe = tmp_path / "io.cpp", tmp_path / "io"
+    src.write_text(IO_DRIVER)
+    cmd = ["g++", "-O1", "-DNX=64", "-DNY=32", "-DNZ=16", "-DINTERACTIONS=0", "-I", os.path.join(root, "include"),
+           "-I", "/usr/local/cuda/include", str(src), "-L", os.path.dirname(gpe_lib), "-lgpe_gb300",
+           "-Wl,-rpath," + os.path.dirname(gpe_lib), "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out = {l.split()[0]: l.split()[1:] for l in r.stdout.splitlines() if l.strip()}
+    assert [float(x) for x in out["NEW"]] == [64, 32, 16, 0.125, 3, 2.5, 1.5, 0.04, 0.0, 1000.0, 12.5]
+    assert [float(x) for x in out["OLD"]] == [8, 16, 32, 0.5, 2, 1.25, 2.0, 0.1, 3.0, 10.0]
+    assert out["TIME"] == ["1", "1"]
+    info = dftc.read_info(str(tmp_path / "run.dftc"))
+    assert (info.system, info.mode, info.nx, info.total_time) == ("fermions", "unitary", 64, 12.5)
+    old = open(tmp_path / "old.dftc.info").read().splitlines()
+    assert len(old) == 10 and old[0] == "8   # nx" and old[3] == "0.500000   # dt"
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("precision", [g.FP64, g.FP32])
 def test_snapshots_match_get_psi(tmp_path, cuda_device, gpe_lib, precision):
