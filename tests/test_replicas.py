@@ -34,7 +34,7 @@ def _worker(rank, ws, port, out):
 def test_replica_rate_is_sum_over_slowest_rank():
     ws = 2
     port = _free_port()
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()  # no fork of this multi-threaded process
     out = mgr.dict()
     mp.spawn(_worker, args=(ws, port, out), nprocs=ws, join=True)
     for rank in range(ws):
