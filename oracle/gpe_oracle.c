@@ -18,6 +18,13 @@
  *   functionals       dev/gpe_user_defined.h:118-135 (UFG), 196-243 (BEC side
  *                     of the crossover), 305-322 (contact BEC)
  *   harmonic trap     dev/gpe_user_defined.h:488-513
+ *   phase enforcing   dev/gpe_engine.cu:465-591, 1112-1477 (gpe_set_vortex, gpe_evolve_vortex*,
+ *                     gpe_get/set_phase, gpe_evolve_enforced_phase)
+ *   currents          dev/gpe_engine.cu:1817-1904
+ *   dipolar BEC       dev/gpe_engine.cu:1481-1809, dev/gpe_user_defined.h:356-451
+ * Pinned: the reference engine's own outputs on the same seeded inputs
+ * (tests/golden, every functional, ITE and RTE, friction, currents, dipolar
+ * evolution and energy) match this restatement to <= 1e-12 relative L2.
  * The 3D FFT is cuFFT Z2Z in the reference (a third-party library absent from
  * the reference tree): unnormalised, e^{-2 pi i jk/n} forward and e^{+...}
  * inverse on a C-order [nx][ny][nz] array.  It is restated here as an
@@ -25,9 +32,11 @@
  * summation over a fixed number of chunks (the reference's tree sum,
  * dev/reductions.cu:64-130, differs only in order).
  *
- * Extension beyond the reference (used by the time-dependent control
- * problem): an optional additive potential table, one real field per time
- * slice, selected by it / steps_per_slice.
+ * Extensions beyond the reference (no reference output pins them; they are
+ * checked against closed forms and numpy restatements in tests/test_oracle.py):
+ * an optional additive potential table, one real field per time slice,
+ * selected by it / steps_per_slice (the time-dependent control problem), and
+ * the Weizsaecker gradient term frozen per step with its sub-steps.
  */
 #include <float.h>
 #include <math.h>
