@@ -32,7 +32,7 @@ class Workload:
 
     @property
     def gamma(self) -> float:
-        return 1.0 if self.interactions == -1 else 2.0
+        return 1.0 if self.interactions < 0 else 2.0  # particles (-1, -2) or dimers (0, 1)
 
 
 def grid(shape, dx=1.0):
