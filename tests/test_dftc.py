@@ -40,6 +40,18 @@ def test_info_reads_a_reference_style_file(tmp_path, gpe_lib):
         dftc.read_info(str(tmp_path / "missing.dftc"))
 
 
+def test_read_frames_layout(tmp_path, gpe_lib):
+    """Frames are consecutive complex128 lattices in C order; the shape comes from the info file."""
+    path = str(tmp_path / "f.dftc")
+    rng = np.random.default_rng(3)
+    frames = rng.standard_normal((3, 8, 4, 16)) + 1j * rng.standard_normal((3, 8, 4, 16))
+    frames.astype(np.complex128).tofile(path)
+    dftc.write_info(path, dftc.Info("bosons", "contact", 8, 4, 16, 0.1, 3, 1.0, 1.0, 0.1, 0.0, 1.0, 0.3))
+    got = dftc.read_frames(path)
+    assert got.shape == (3, 8, 4, 16) and np.array_equal(got, frames)
+    assert np.array_equal(dftc.read_frames(path, shape=(16, 4, 8))[2], frames[2].reshape(16, 4, 8))
+
+
 IO_DRIVER = r"""
 #include <cstdio>
 #include <cstring>
