@@ -47,6 +47,23 @@ def peaks():
         return 6800.0, "fallback"
 
 
+FP64_PEAK_TFLOPS = 1.25  # nominal GB300 FP64 rate (no measured figure)
+
+
+def fp64_rooflines(steps_per_s, n_points, qf=True):
+    """Both bounds of the FP64 form at `steps_per_s`: HBM (B_alg bytes per point per step) and the FP64
+    ALU (F_alg = n_fft 5 N log2 N + 60 N flops per step: n_fft = 8 3D transforms with quantum friction,
+    4 without, plus the pointwise phases).  The binding one is the larger fraction."""
+    hbm, kind = peaks()
+    gbs = B_ALG[("fp64", qf)] * n_points * steps_per_s / 1e9
+    n_fft = 8 if qf else 4
+    flops = n_fft * 5.0 * n_points * float(np.log2(n_points)) + 60.0 * n_points
+    tf = flops * steps_per_s / 1e12
+    return {"hbm": {"achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm, "peak_kind": kind},
+            "fp64_alu": {"achieved": tf, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": tf / FP64_PEAK_TFLOPS,
+                         "peak_kind": "nominal", "flops_per_step": flops}}
+
+
 class Clocks:
     """Samples SM clocks and throttle reasons with nvidia-smi while running."""
 
@@ -665,7 +682,8 @@ def main():
         e64 = make_engine(w, psi, g.FP64)
         b64 = max(5, args.block // 10)
         t64, _ = time_blocks(e64, b64, 3, 1, flush, torch)
-        extras["fp64_plain"] = {"value": 3 * b64 / t64, "unit": "steps/s", "dtype": "f64"}
+        extras["fp64_plain"] = {"value": 3 * b64 / t64, "unit": "steps/s", "dtype": "f64",
+                                "roofline": fp64_rooflines(3 * b64 / t64, int(np.prod(w.shape)), qf=w.qf != 0.0)}
         # FP32 energy and density error against the FP64 form after the same steps
         a = make_engine(w, psi, g.FP32)
         b = make_engine(w, psi, g.FP64)

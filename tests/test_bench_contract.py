@@ -25,3 +25,18 @@ def test_reference_arm_prints_one_contract_line():
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
     assert d["config"]["workload"] and d["config"]["lattice"] == [128, 128, 128]
+
+
+def test_fp64_rooflines_arithmetic():
+    """FP64 form at 128^3 with friction: 240 B/pt and 8 * 5 N log2 N + 60 N flops per step."""
+    sys.path.insert(0, ROOT)
+    import bench
+    n = 128 ** 3
+    r = bench.fp64_rooflines(100.0, n, qf=True)
+    assert r["hbm"]["achieved"] == 240 * n * 100.0 / 1e9
+    assert r["fp64_alu"]["flops_per_step"] == 8 * 5.0 * n * 21 + 60.0 * n
+    assert abs(r["fp64_alu"]["achieved"] - r["fp64_alu"]["flops_per_step"] * 100.0 / 1e12) < 1e-12
+    assert r["fp64_alu"]["frac"] == r["fp64_alu"]["achieved"] / bench.FP64_PEAK_TFLOPS
+    plain = bench.fp64_rooflines(100.0, n, qf=False)
+    assert plain["hbm"]["achieved"] == 176 * n * 100.0 / 1e9
+    json.dumps(r)
