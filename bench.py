@@ -47,21 +47,30 @@ def peaks():
         return 6800.0, "fallback"
 
 
-FP64_PEAK_TFLOPS = 1.25  # nominal GB300 FP64 rate (no measured figure)
-
-
-def fp64_rooflines(steps_per_s, n_points, qf=True):
+def fp64_rooflines(steps_per_s, n_points, fp64_peak, qf=True):
     """Both bounds of the FP64 form at `steps_per_s`: HBM (B_alg bytes per point per step) and the FP64
-    ALU (F_alg = n_fft 5 N log2 N + 60 N flops per step: n_fft = 8 3D transforms with quantum friction,
-    4 without, plus the pointwise phases).  The binding one is the larger fraction."""
+    ALU (F_alg = n_fft 5 N log2 N + 60 N flops per step: n_fft = 6 3D-transform equivalents with quantum
+    friction -- the 18 axis transforms the engine runs, the friction Laplacian computed once per step --
+    and 4 without, plus the pointwise phases).  `fp64_peak` = (TFLOP/s, kind).  The binding bound is the
+    larger fraction."""
     hbm, kind = peaks()
     gbs = B_ALG[("fp64", qf)] * n_points * steps_per_s / 1e9
-    n_fft = 8 if qf else 4
+    n_fft = 6 if qf else 4
     flops = n_fft * 5.0 * n_points * float(np.log2(n_points)) + 60.0 * n_points
     tf = flops * steps_per_s / 1e12
+    peak_tf, peak_kind = fp64_peak
     return {"hbm": {"achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm, "peak_kind": kind},
-            "fp64_alu": {"achieved": tf, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": tf / FP64_PEAK_TFLOPS,
-                         "peak_kind": "nominal", "flops_per_step": flops}}
+            "fp64_alu": {"achieved": tf, "peak": peak_tf, "unit": "TFLOP/s", "frac": tf / peak_tf,
+                         "peak_kind": peak_kind, "flops_per_step": flops, "fft_equivalents_per_step": n_fft}}
+
+
+def measured_fp64_peak():
+    """FP64 FMA rate of this GPU measured now (independent DFMA chains, CUDA events)."""
+    import libcugpe_gb300 as g
+    try:
+        return g.fp64_fma_rate(), "measured (DFMA-chain kernel, best of 5 launches, this run)"
+    except Exception as ex:  # reported, never fatal
+        return 1.25, f"nominal (measurement failed: {str(ex)[:80]})"
 
 
 class Clocks:
@@ -161,16 +170,17 @@ def whole_job_rate(ws, units_per_rank, seconds_this_rank):
 
 
 def traffic_from_profiles(n):
-    """ncu DRAM bytes per step of the pass kernels for this lattice, from profiles/ (or None)."""
+    """DRAM bytes per GPE step of the pass kernels for this lattice, from the ncu summary under
+    profiles/ ((bytes, how it was captured) or (None, None))."""
     path = os.path.join(ROOT, "profiles", "pass_kernel_traffic.txt")
     try:
         for line in open(path):
-            f = line.split()
+            f = line.split(None, 2)
             if len(f) >= 2 and f[0] == f"fp32_ufg_qf_rte_{n}":
-                return float(f[1])
+                return float(f[1]), (f[2].strip() if len(f) > 2 else "")
     except OSError:
         pass
-    return None
+    return None, None
 
 
 def workload(n):
@@ -437,7 +447,8 @@ def run_batch_workload(args):
         per_size[n] = {"count": sum(1 for c in ens if c["shape"][0] == n), "timed": len(idx),
                        "mean_s": float(np.mean(times)), "mu_rel_err_fp32_vs_fp64": float(max(errs)) if errs else None}
     t_serial = sum(v["count"] * v["mean_s"] for v in per_size.values())
-    line = {"metric": "batched ITE ensemble solves/s (96 BEC ground states: 32x32^3, 48x64^3, 16x128^3)",
+    line = {"metric": "batched ITE ensemble solves/s (96 BEC ground states: 32x32^3, 48x64^3, 16x128^3); "
+                      f"serial FP64 loop timed on the first {subset} condensates of each size, extrapolated",
             "value": len(ens) / t_batch, "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
             "dtype": "f32", "data": "synthetic (seeded)", "converged": int(done.sum()), "of": len(ens),
             "batch_seconds": t_batch, "steps_max": int(steps.max()), "gpu_launches": int(launches),
@@ -455,7 +466,7 @@ def run_batch_workload(args):
             "config": {"workload": "ensemble of 96 BEC ITE solves (32 at 32^3, 48 at 64^3, 16 at 128^3), gN~U[50,500], omega_z/omega_perp~U[0.8,1.25], "
                                    "width~U[0.8,1.2], box 16 (dx=16/n), dt=5e-3; converged when the mean of mu over a "
                                    "25-step interval changes by < 1e-8 per step between intervals"}}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def run_bec64_workload(args):
@@ -491,7 +502,7 @@ def run_bec64_workload(args):
                                              "(its synchronous D2H per step)"}
     except Exception as ex:
         line["reference_gpu"] = {"unavailable": str(ex)[:200]}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def run_cool512_workload(args):
@@ -551,7 +562,7 @@ def run_cool512_workload(args):
             "config": {"workload": "cooling run: 512^3, dx=0.1, UFG, quantum friction 0.2, omega=1, 8 vortex lines "
                                    "(charge +1, seeded in the disk r<4), dt=2e-3, %d steps, npart=5e4"
                                    % w.steps, "lattice": list(w.shape)}}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def run_control_workload(args):
@@ -613,8 +624,31 @@ def run_control_workload(args):
             "config": {"workload": "optimal control of an RTE BEC: 64^3, dx=0.25, gN=200, omega=1, dt=1e-3, 2000 steps, 16 Gaussians "
                                    "sigma=0.8 centres U[-3,3]^3, 100 slices, controls N(0,0.05), target = ground state "
                                    "of the trap shifted by (0.5,0,0), checkpoints every 100 steps"}}
-    print(json.dumps(line), flush=True)
     cp.close()
+    return line
+
+
+def run_lattice_workload(args):
+    """A seeded FP32-mixed (or FP64) UFG + quantum friction real-time run on any lattice, for kernel
+    profilers: `--warm` steps (the first step runs 8 fused passes, every later one 7), then `--steps`
+    more, so that `ncu -k regex:pass_kernel -s <7*warm+1> -c <7*steps>` captures whole steady steps."""
+    import libcugpe_gb300 as g
+    from libcugpe_gb300 import configs
+    shape = tuple(int(x) for x in args.lattice.split(","))
+    prec = g.FP32 if args.precision == "fp32" else g.FP64
+    e = g.Engine(shape, 0, 1.0, 0.0, 0.02, 1e5, precision=prec)
+    e.set_user_params([0.002, 0.002, 0.003, 0.0])
+    e.set_quantum_friction_coeff(0.1)
+    e.set_psi(0.0, configs.random_state(shape, seed=3, npart=1e5, gamma=2.0))
+    e.evolve_qf(args.warm)
+    e.synchronize()
+    t0 = time.perf_counter()
+    e.evolve_qf(args.steps)
+    e.synchronize()
+    secs = time.perf_counter() - t0
+    e.close()
+    return {"metric": "seeded run for profilers (wall clock, not a benchmark)", "lattice": list(shape),
+            "precision": args.precision, "steps": args.steps, "seconds": secs}
 
 
 def main():
@@ -626,10 +660,15 @@ def main():
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--block", type=int, default=100)
     ap.add_argument("--cpu-steps", type=int, default=2)
-    ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="only the headline line (profiling runs)")
     ap.add_argument("--ite-steps", type=int, default=200)
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--workload", default="ufg_qf", choices=["ufg_qf", "batch", "control", "bec64", "cool512"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--fp32-check-steps", type=int, default=10000)
+    ap.add_argument("--workload", default="ufg_qf",
+                    choices=["ufg_qf", "batch", "control", "bec64", "cool512", "lattice"])
+    ap.add_argument("--lattice", default="512,512,128")
+    ap.add_argument("--warm", type=int, default=3)
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--cool-steps", type=int, default=5000)
     ap.add_argument("--control-steps", type=int, default=2000)
     ap.add_argument("--control-ckpt", type=int, default=100)
@@ -638,17 +677,10 @@ def main():
     ap.add_argument("--batch-serial-subset", type=int, default=2)
     ap.add_argument("--batch-diag", type=int, default=4)
     args = ap.parse_args()
-    if args.workload == "batch":
-        run_batch_workload(args)
-        return
-    if args.workload == "control":
-        run_control_workload(args)
-        return
-    if args.workload == "bec64":
-        run_bec64_workload(args)
-        return
-    if args.workload == "cool512":
-        run_cool512_workload(args)
+    single = {"batch": run_batch_workload, "control": run_control_workload, "bec64": run_bec64_workload,
+              "cool512": run_cool512_workload, "lattice": run_lattice_workload}
+    if args.workload in single:
+        print(json.dumps(single[args.workload](args)), flush=True)
         return
     ws, rank, local = dist_setup()
     if args.impl == "reference":
@@ -668,7 +700,7 @@ def main():
         t32, launches = time_blocks(e32, args.block, args.steps, args.warmup, flush, torch)
     value = whole_job_rate(ws, args.steps * args.block, t32)
     t32 = max_over_ranks(ws, t32)
-    # per-pass kernel times (CUDA events around each fused pass, engine stream)
+    # per-pass kernel times (CUDA events around each fused pass, engine stream): shares of the step
     passes = e32.profile_passes(20)
 
     host = torch.empty(w.shape + (2,), dtype=torch.float64, pin_memory=True).numpy().view(np.complex128)[..., 0]
@@ -678,16 +710,18 @@ def main():
 
     extras = {}
     if not args.no_extras and rank == 0:
-        # plain FP64 drop-in on the same workload
+        # plain FP64 drop-in on the same workload, with both of its rooflines (FP64 peak measured now)
         e64 = make_engine(w, psi, g.FP64)
         b64 = max(5, args.block // 10)
         t64, _ = time_blocks(e64, b64, 3, 1, flush, torch)
         extras["fp64_plain"] = {"value": 3 * b64 / t64, "unit": "steps/s", "dtype": "f64",
-                                "roofline": fp64_rooflines(3 * b64 / t64, int(np.prod(w.shape)), qf=w.qf != 0.0)}
-        # FP32 energy and density error against the FP64 form after the same steps
+                                "roofline": fp64_rooflines(3 * b64 / t64, int(np.prod(w.shape)),
+                                                           measured_fp64_peak(), qf=w.qf != 0.0)}
+        e64.close()
+        # FP32 energy and density error against the FP64 form over the workload's full run
         a = make_engine(w, psi, g.FP32)
         b = make_engine(w, psi, g.FP64)
-        nchk = 200
+        nchk = args.fp32_check_steps
         a.evolve_qf(nchk)
         b.evolve_qf(nchk)
         ea, eb = a.energy(), b.energy()
@@ -696,7 +730,7 @@ def main():
         _, db = b.get_density()
         extras["fp32_vs_fp64"] = {"steps": nchk, "dE_over_E": abs(Ea - Eb) / abs(Eb),
                                   "density_rel_l2": float(np.linalg.norm(da - db) / np.linalg.norm(db))}
-        a.close(); b.close(); e64.close()
+        a.close(); b.close()
         # the workload with its Weizsaecker gradient term of weight 0.25 (not in the reference:
         # pinned by the oracle only); FP32 speed and FP32-vs-FP64 error after the same steps
         aw = make_engine(w, psi, g.FP32)
@@ -705,29 +739,49 @@ def main():
         aw.set_psi(0.0, psi)
         bw = make_engine(w, psi, g.FP64)
         bw.set_weizsacker(0.25)
-        aw.evolve_qf(nchk)
-        bw.evolve_qf(nchk)
+        nwz = 200
+        aw.evolve_qf(nwz)
+        bw.evolve_qf(nwz)
         ea, eb = aw.energy(), bw.energy()
         Ea, Eb = sum(ea[1:]), sum(eb[1:])
         _, da = aw.get_density()
         _, db = bw.get_density()
         extras["weizsacker_0.25"] = {
             "value": max(2, args.steps // 2) * args.block / tw, "unit": "steps/s", "dtype": "f32",
-            "fp32_vs_fp64": {"steps": nchk, "dE_over_E_without_EW": abs(Ea - Eb) / abs(Eb),
+            "fp32_vs_fp64": {"steps": nwz, "dE_over_E_without_EW": abs(Ea - Eb) / abs(Eb),
                              "density_rel_l2": float(np.linalg.norm(da - db) / np.linalg.norm(db))}}
         aw.close(); bw.close()
         ref = reference_gpu(w, psi)
         if ref:
             extras["reference_gpu"] = ref
         extras["cpu_baseline"] = cpu_baseline(w, psi, seconds=args.cpu_seconds)
+        # the other workloads of the benchmark set, each with its own value and checks
+        for key, fn in (("bec64_ite", run_bec64_workload), ("batch_ensemble", run_batch_workload),
+                        ("control_adjoint", run_control_workload), ("cool512", run_cool512_workload)):
+            t_w = time.perf_counter()
+            try:
+                extras[key] = fn(args)
+            except Exception as ex:  # reported, never fatal
+                extras[key] = {"unavailable": f"{type(ex).__name__}: {str(ex)[:300]}"}
+            extras[key]["wall_s"] = round(time.perf_counter() - t_w, 1)
 
     if rank == 0:
         n = int(np.prod(w.shape))
         peak, kind = peaks()
-        step_kernel_s = sum(p["ms"] for p in passes) / 1e3
-        achieved = B_ALG[("fp32", True)] * n / step_kernel_s / 1e9
-        top = max(passes, key=lambda p: p["ms"])
-        traffic = traffic_from_profiles(w.shape[0])
+        # the roofline follows from the timed number: one GPE step = ms_per_step / block
+        gpe_step_s = t32 / (args.steps * args.block)
+        achieved = B_ALG[("fp32", True)] * n / gpe_step_s / 1e9
+        # per-pass CUDA-event times (measured with an event between passes, which breaks the overlap of
+        # programmatic dependent launch) serve as shares of the timed step
+        ev_total = sum(p["ms"] for p in passes)
+        per_pass = []
+        for p in passes:
+            share = p["ms"] / ev_total
+            us = share * gpe_step_s * 1e6
+            per_pass.append({"axis": p["axis"], "kind": p["kind"], "share": round(share, 4),
+                             "us_in_step": round(us, 2), "own_bytes_GBps": round(p["bytes"] / (us / 1e6) / 1e9, 1)})
+        top = max(per_pass, key=lambda p: p["share"])
+        traffic, traffic_how = traffic_from_profiles(w.shape[0])
         clk_s = clk.summary()
         line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * t32 / args.steps, "higher_is_better": True,
@@ -735,16 +789,14 @@ def main():
                 "config": config_obj(w, args),
                 "points_steps_per_s": value * n,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "traffic": traffic,
-                             "kernel": "pass_kernel (fused pencil pass; 7 launches per step)",
-                             "basis": f"B_alg {B_ALG[('fp32', True)]} B/pt/step x {n} pts / summed pass time "
-                                      f"{1e6 * step_kernel_s:.1f} us per step (CUDA events); peak {kind}; "
-                                      "traffic = ncu dram bytes per step",
-                             "per_pass": [{"axis": p["axis"], "kind": p["kind"], "us": round(1e3 * p["ms"], 2),
-                                           "GBps": round(p["bytes"] / (p["ms"] / 1e3) / 1e9, 1)} for p in passes],
-                             "top_pass": {"axis": top["axis"], "kind": top["kind"],
-                                          "achieved_GBps": top["bytes"] / (top["ms"] / 1e3) / 1e9,
-                                          "frac": top["bytes"] / (top["ms"] / 1e3) / 1e9 / peak}},
+                             "frac": achieved / peak, "traffic": traffic, "traffic_how": traffic_how,
+                             "kernel": "pass_kernel (fused pencil pass; 7 launches per GPE step)",
+                             "basis": f"B_alg {B_ALG[('fp32', True)]} B/pt/step x {n} pts / {1e6 * gpe_step_s:.2f} us "
+                                      f"per GPE step (= ms_per_step / {args.block}, CUDA events on the engine "
+                                      f"stream); peak {kind}; traffic = ncu DRAM bytes per GPE step",
+                             "per_pass": per_pass,
+                             "top_pass": top,
+                             "per_pass_event_sum_us": round(1e3 * ev_total, 2)},
                 "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": 16 * n,
                         "d2h_bytes_per_step": 16 * n},
                 "gpu_launches": launches, "clocks": clk_s}

@@ -136,6 +136,10 @@ int gpe_gb_use_graphs(gpe_gb_engine* e, int enable);
  * nx*ny*nz doubles; step `it` uses slice min(it / steps_per_slice, nslices-1)
  * on top of the harmonic trap.  NULL removes it. */
 int gpe_gb_set_potential_slices(gpe_gb_engine* e, const double* fields, int nslices, int steps_per_slice);
+/* Measured FP64 fused multiply-add rate of the current device in TFLOP/s
+ * (no reference counterpart; a measurement aid for the FP64 form's ALU
+ * roofline): independent FMA chains, CUDA events, best of five launches. */
+int gpe_gb_fp64_fma_rate(double* tflops);
 /* Allocation-free norm (no counterpart in the reference library).
  * For callers that cannot allocate device memory when they need the norm:
  * code running while its stream is captured into a CUDA graph, applications
@@ -148,7 +152,9 @@ int gpe_gb_set_potential_slices(gpe_gb_engine* e, const double* fields, int nsli
  * GPU that loads the library until the process exits.  At most 2^27 points
  * (512^3); more returns GPE_ERR_NOALLOC_SIZE.  The first call on a device
  * looks up the scratch address (cudaGetSymbolAddress) and must come before
- * any stream capture.  All calls share the scratch: calls whose kernels can
+ * any stream capture; the address is kept for the life of the device's
+ * primary context, so do not call this entry point on a device again after
+ * cudaDeviceReset of that device.  All calls share the scratch: calls whose kernels can
  * overlap on the GPU (different streams, or host threads) race and must be
  * serialised by the caller. */
 int gpe_gb_norm_noalloc(const void* psi, int precision, long long n, double gamma, double* norm_out, void* stream);

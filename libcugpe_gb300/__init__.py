@@ -50,7 +50,7 @@ C_ABI_SYMBOLS = [
     "gpe_gb_control_loss_grad", "gpe_gb_control_destroy", "gpe_gb_snapshots_open", "gpe_gb_snapshots_push",
     "gpe_gb_snapshots_close", "gpe_gb_dftc_write_info", "gpe_gb_dftc_read_info", "gpe_gb_set_weizsacker",
     "gpe_gb_evolve_dipolar", "gpe_gb_energy_dipolar", "gpe_gb_autotune", "gpe_gb_batch_autotune",
-    "gpe_gb_set_fft_plan", "gpe_gb_get_fft_plan", "gpe_gb_batch_set_fft_plan",
+    "gpe_gb_set_fft_plan", "gpe_gb_get_fft_plan", "gpe_gb_batch_set_fft_plan", "gpe_gb_fp64_fma_rate",
 ]
 
 
@@ -106,6 +106,7 @@ def _lib():
             "gpe_gb_error_string": (ctypes.c_char_p, [i]),
             "gpe_gb_get_stream": (vp, [vp]),
             "gpe_gb_norm_noalloc": (i, [vp, i, ctypes.c_longlong, d, vp, vp]),
+            "gpe_gb_fp64_fma_rate": (i, [dp]),
             "gpe_gb_set_vortex": (i, [vp, d, d, i]),
             "gpe_gb_get_phase": (i, [vp, dp]),
             "gpe_gb_set_phase": (i, [vp, dp]),
@@ -142,6 +143,13 @@ def _lib():
 
 def lib_path() -> str:
     return LIB_PATH
+
+
+def fp64_fma_rate() -> float:
+    """Measured FP64 FMA throughput of the current device, TFLOP/s."""
+    r = ctypes.c_double()
+    _check(_lib().gpe_gb_fp64_fma_rate(ctypes.byref(r)), "fp64_fma_rate")
+    return r.value
 
 
 def _dp(a: np.ndarray):

@@ -43,6 +43,7 @@ def _sources():
         units.append(path)
     units.append(os.path.join(CSRC, "gpe_engine.cu"))
     units.append(os.path.join(CSRC, "gpe_noalloc.cu"))
+    units.append(os.path.join(CSRC, "gpe_probe.cu"))
     units.append(os.path.join(CSRC, "gpe_batch_kernels.cu"))
     units.append(os.path.join(CSRC, "gpe_dropin.cpp"))
     units.append(os.path.join(CSRC, "gpe_snapshots.cpp"))

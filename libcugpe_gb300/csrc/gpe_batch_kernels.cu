@@ -1,27 +1,32 @@
 // Instantiation of the batched pass kernels (FP32-mixed form) and their
 // launch dispatch over (axis, kernel class, radix plan).
 #include "gpe_batch.cuh"
+#include "gpe_device_state.h"
 
 namespace gpe {
 
 template <typename R, int AX, int CLS, int P>
 static cudaError_t launch_b(const BatchItem<R>* items, int nitems, unsigned grid, size_t smem, cudaStream_t st) {
-    static bool configured = false;  // single device
-    if (!configured) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    // kernel attributes belong to the device context: set them once per device
+    static DeviceOnce configured;
+    const int rc = configured.ensure(dev, [] {
         size_t mx = PassGeom<R, 32, AX, kBatchThreads, P>::SMEM_MAX;
         if (PassGeom<R, 64, AX, kBatchThreads, P>::SMEM_MAX > mx) mx = PassGeom<R, 64, AX, kBatchThreads, P>::SMEM_MAX;
         if (PassGeom<R, 128, AX, kBatchThreads, P>::SMEM_MAX > mx)
             mx = PassGeom<R, 128, AX, kBatchThreads, P>::SMEM_MAX;
         if (PassGeom<R, 256, AX, kBatchThreads, P>::SMEM_MAX > mx)
             mx = PassGeom<R, 256, AX, kBatchThreads, P>::SMEM_MAX;
-        cudaError_t e = cudaFuncSetAttribute(pass_batch_kernel<R, AX, CLS, P>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx);
-        if (e != cudaSuccess) return e;
-        e = cudaFuncSetAttribute(pass_batch_kernel<R, AX, CLS, P>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 (int)cudaSharedmemCarveoutMaxShared);
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+        cudaError_t e2 = cudaFuncSetAttribute(pass_batch_kernel<R, AX, CLS, P>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx);
+        if (e2 == cudaSuccess)
+            e2 = cudaFuncSetAttribute(pass_batch_kernel<R, AX, CLS, P>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                      (int)cudaSharedmemCarveoutMaxShared);
+        return (int)e2;
+    }, (int)cudaErrorInvalidDevice);
+    if (rc) return (cudaError_t)rc;
     pass_batch_kernel<R, AX, CLS, P><<<grid, kBatchThreads, smem, st>>>(items, nitems);
     return cudaGetLastError();
 }

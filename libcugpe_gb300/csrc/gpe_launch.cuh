@@ -4,6 +4,7 @@
 // unit per (precision, pencil length) so they compile in parallel.
 #pragma once
 #include <cuda_runtime.h>
+#include "gpe_device_state.h"
 #include "gpe_pass.cuh"
 
 namespace gpe {
@@ -24,32 +25,40 @@ template <typename R, int N, int AX, int P = 0> constexpr int pass_nt() {
 template <typename R, int N, int AX, int NT, int CLS, int P>
 cudaError_t launch_one(const PassArgs<R>& a, size_t pencils, cudaStream_t st) {
     using Geo = PassGeom<R, N, AX, NT, P>;
-    static bool configured = false;  // per instantiation, single device
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(pass_kernel<R, N, AX, NT, CLS, P>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Geo::SMEM_MAX);
-        if (e != cudaSuccess) return e;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    // kernel attributes belong to the device context: set them once per device
+    static DeviceOnce configured;
+    int rc = configured.ensure(dev, [] {
+        cudaError_t e2 = cudaFuncSetAttribute(pass_kernel<R, N, AX, NT, CLS, P>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Geo::SMEM_MAX);
         // the passes use shared memory, not L1, for reuse: ask for the largest carveout
-        e = cudaFuncSetAttribute(pass_kernel<R, N, AX, NT, CLS, P>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 (int)cudaSharedmemCarveoutMaxShared);
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
+        if (e2 == cudaSuccess)
+            e2 = cudaFuncSetAttribute(pass_kernel<R, N, AX, NT, CLS, P>,
+                                      cudaFuncAttributePreferredSharedMemoryCarveout,
+                                      (int)cudaSharedmemCarveoutMaxShared);
+        return (int)e2;
+    }, (int)cudaErrorInvalidDevice);
+    if (rc) return (cudaError_t)rc;
     unsigned grid = (unsigned)((pencils + Geo::W - 1) / Geo::W);
     size_t smem = Geo::SMEM_BASE + slot_bytes<R>(staged_ops(a.mid, a.post, a.flags), Geo::E * NT);
     if constexpr (CLS == C_KINP) {
-        // persistent: one staging buffer per CTA, as many CTAs as fit on the GPU at once
+        // persistent: one staging buffer per CTA, as many CTAs as fit on the device at once
         smem = Geo::SMEM_BASE + (size_t)Geo::E * NT * sizeof(C2<R>);
-        static unsigned resident = 0;  // per instantiation, single device
-        if (!resident) {
-            int per_sm = 0, sms = 0, dev = 0;
-            cudaError_t e = cudaGetDevice(&dev);
-            if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            if (e == cudaSuccess)
-                e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pass_kernel<R, N, AX, NT, CLS, P>, NT, smem);
-            if (e != cudaSuccess) return e;
-            resident = (unsigned)((per_sm > 0 ? per_sm : 1) * sms);
-        }
+        static DeviceValue<unsigned> resident_ctas;
+        unsigned resident = 0;
+        rc = resident_ctas.ensure(dev, &resident, [dev, smem](unsigned* out) {
+            int per_sm = 0, sms = 0;
+            cudaError_t e2 = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (e2 == cudaSuccess)
+                e2 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pass_kernel<R, N, AX, NT, CLS, P>, NT,
+                                                                   smem);
+            if (e2 != cudaSuccess) return (int)e2;
+            *out = (unsigned)((per_sm > 0 ? per_sm : 1) * sms);
+            return 0;
+        }, (int)cudaErrorInvalidDevice);
+        if (rc) return (cudaError_t)rc;
         if (grid > resident) grid = resident;
     }
     if (smem > Geo::SMEM_MAX) return cudaErrorInvalidConfiguration;  // more staged operands than a CTA holds

@@ -14,18 +14,22 @@
 // __device__ array of fixed size, held by every GPU that loads the library
 // until the process exits.  Host code cannot use the array's name as a
 // device address; the first call on each device looks the address up with
-// cudaGetSymbolAddress while that device is current and keeps it.
+// cudaGetSymbolAddress while that device is current and keeps it, so that
+// first call belongs before any stream capture.  The kept address is valid
+// for the life of the device's primary context: after cudaDeviceReset the
+// module is loaded again and the array may move, so a process that resets a
+// device must not call this entry point on that device again.
 #include <cuda_runtime.h>
 #include <math.h>
 
 #include "../../include/gpe_gb300.h"
+#include "gpe_device_state.h"
 
 namespace {
 
 constexpr int kNaBlocks = 512;
 constexpr int kNaThreads = 256;
 constexpr long long kNaMaxPoints = 1LL << 27;  // 512^3, the engine's largest lattice
-constexpr int kNaMaxDevices = 64;
 
 struct NaScratch {
     double partials[kNaBlocks];
@@ -36,7 +40,9 @@ struct NaScratch {
 // 4 KiB of partial sums + 256 B for the ticket
 static __device__ __align__(256) NaScratch g_na_scratch;
 
-static NaScratch* g_na_addr[kNaMaxDevices] = {nullptr};
+// device address of g_na_scratch per device ordinal (host threads may race to fill an entry: they
+// store the same value)
+static gpe::DeviceValue<NaScratch*> g_na_addr;
 
 template <typename C>
 __global__ void __launch_bounds__(kNaThreads) k_norm_noalloc(const C* __restrict__ psi, long long n, double gamma,
@@ -78,15 +84,13 @@ int scratch_for_current_device(NaScratch** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return (int)e;
-    if (dev < 0 || dev >= kNaMaxDevices) return GPE_ERR_ARGUMENT;
-    if (!g_na_addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_na_scratch);
-        if (e != cudaSuccess) return (int)e;
-        g_na_addr[dev] = static_cast<NaScratch*>(p);
-    }
-    *out = g_na_addr[dev];
-    return 0;
+    return g_na_addr.ensure(dev, out, [](NaScratch** p) {
+        void* a = nullptr;
+        const cudaError_t e2 = cudaGetSymbolAddress(&a, g_na_scratch);
+        if (e2 != cudaSuccess) return (int)e2;
+        *p = static_cast<NaScratch*>(a);
+        return 0;
+    }, GPE_ERR_ARGUMENT);
 }
 
 }  // namespace

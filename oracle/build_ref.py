@@ -37,7 +37,23 @@ import sys
 from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("GPE_REFERENCE_ROOT", "/root/reference")
+
+
+def _reference_root() -> str:
+    """The reference checkout: $GPE_REFERENCE_ROOT, else the `reference_path` recorded in the
+    repository's benchmark spec; empty when neither names one."""
+    root = os.environ.get("GPE_REFERENCE_ROOT", "")
+    if root:
+        return root
+    try:
+        import json
+        with open(os.path.join(os.path.dirname(HERE), "BASELINE.json")) as fh:
+            return str(json.load(fh).get("reference_path", "") or "")
+    except (OSError, ValueError):
+        return ""
+
+
+REF_ROOT = _reference_root()
 OUT = os.path.join(HERE, "_ref")
 SRC = os.path.join(OUT, "src")
 BIN = os.path.join(OUT, "bin")
@@ -74,8 +90,8 @@ def _edit(name: str, text: str) -> str:
 
 
 def prepare() -> bool:
-    dev = os.path.join(REF_ROOT, "dev")
-    if not os.path.isdir(dev):
+    dev = os.path.join(REF_ROOT, "dev") if REF_ROOT else ""
+    if not dev or not os.path.isdir(dev):
         return os.path.isfile(os.path.join(SRC, "gpe_engine.cu"))
     os.makedirs(SRC, exist_ok=True)
     for f in FILES:

@@ -28,15 +28,30 @@ def test_reference_arm_prints_one_contract_line():
 
 
 def test_fp64_rooflines_arithmetic():
-    """FP64 form at 128^3 with friction: 240 B/pt and 8 * 5 N log2 N + 60 N flops per step."""
+    """FP64 form at 128^3 with friction: 240 B/pt and 6 * 5 N log2 N + 60 N flops per step (the 18 axis
+    transforms of a friction step are 6 3D-transform equivalents); without friction 176 B/pt and 4."""
     sys.path.insert(0, ROOT)
     import bench
     n = 128 ** 3
-    r = bench.fp64_rooflines(100.0, n, qf=True)
+    peak = (1.5, "measured")
+    r = bench.fp64_rooflines(100.0, n, peak, qf=True)
     assert r["hbm"]["achieved"] == 240 * n * 100.0 / 1e9
-    assert r["fp64_alu"]["flops_per_step"] == 8 * 5.0 * n * 21 + 60.0 * n
+    assert r["fp64_alu"]["flops_per_step"] == 6 * 5.0 * n * 21 + 60.0 * n
     assert abs(r["fp64_alu"]["achieved"] - r["fp64_alu"]["flops_per_step"] * 100.0 / 1e12) < 1e-12
-    assert r["fp64_alu"]["frac"] == r["fp64_alu"]["achieved"] / bench.FP64_PEAK_TFLOPS
-    plain = bench.fp64_rooflines(100.0, n, qf=False)
+    assert r["fp64_alu"]["frac"] == r["fp64_alu"]["achieved"] / 1.5
+    assert r["fp64_alu"]["peak_kind"] == "measured"
+    plain = bench.fp64_rooflines(100.0, n, peak, qf=False)
     assert plain["hbm"]["achieved"] == 176 * n * 100.0 / 1e9
+    assert plain["fp64_alu"]["flops_per_step"] == 4 * 5.0 * n * 21 + 60.0 * n
     json.dumps(r)
+
+
+def test_traffic_summary_is_read_with_its_label(tmp_path, monkeypatch):
+    sys.path.insert(0, ROOT)
+    import bench
+    prof = tmp_path / "profiles"
+    prof.mkdir()
+    (prof / "pass_kernel_traffic.txt").write_text("# comment\nfp32_ufg_qf_rte_128 1.5e8 steady state, cache-control none\n")
+    monkeypatch.setattr(bench, "ROOT", str(tmp_path))
+    assert bench.traffic_from_profiles(128) == (1.5e8, "steady state, cache-control none")
+    assert bench.traffic_from_profiles(256) == (None, None)
