@@ -136,6 +136,11 @@ int gpe_gb_use_graphs(gpe_gb_engine* e, int enable);
  * nx*ny*nz doubles; step `it` uses slice min(it / steps_per_slice, nslices-1)
  * on top of the harmonic trap.  NULL removes it. */
 int gpe_gb_set_potential_slices(gpe_gb_engine* e, const double* fields, int nslices, int steps_per_slice);
+/* Whether this library was built with a user hook header (include/gpe_user_defined.h;
+ * no reference counterpart: the reference recompiles instead): *enabled = 1 and
+ * *interactions = the functional the hooks were compiled for (gpe_gb_create
+ * refuses any other), else *enabled = 0. */
+int gpe_gb_user_hooks(int* enabled, int* interactions);
 /* Measured FP64 fused multiply-add rate of the current device in TFLOP/s
  * (no reference counterpart; a measurement aid for the FP64 form's ALU
  * roofline): independent FMA chains, CUDA events, best of five launches. */

@@ -1,9 +1,19 @@
-// Instantiation of the batched pass kernels (FP32-mixed form) and their
-// launch dispatch over (axis, kernel class, radix plan).
+// Batched pass kernels (FP32-mixed form): launch per (axis, kernel class,
+// radix plan).  One generated translation unit per (axis, plan) defines
+// GPE_BATCH_DEFINITIONS and instantiates launch_bc for it, so they compile in
+// parallel; the dispatch over axis and plan (launch_batch) is in
+// gpe_batch_dispatch.cu.  A library built without the batched solver defines
+// GPE_BATCH_STUBS instead: every batched pass is then refused.
+#pragma once
 #include "gpe_batch.cuh"
 #include "gpe_device_state.h"
 
 namespace gpe {
+
+template <typename R, int AX, int P>
+cudaError_t launch_bc(int cls, const BatchItem<R>* items, int nitems, unsigned grid, size_t smem, cudaStream_t st);
+
+#ifdef GPE_BATCH_DEFINITIONS
 
 template <typename R, int AX, int CLS, int P>
 static cudaError_t launch_b(const BatchItem<R>* items, int nitems, unsigned grid, size_t smem, cudaStream_t st) {
@@ -32,8 +42,8 @@ static cudaError_t launch_b(const BatchItem<R>* items, int nitems, unsigned grid
 }
 
 template <typename R, int AX, int P>
-static cudaError_t launch_bc(int cls, const BatchItem<R>* items, int nitems, unsigned grid, size_t smem,
-                             cudaStream_t st) {
+cudaError_t launch_bc(int cls, const BatchItem<R>* items, int nitems, unsigned grid, size_t smem,
+                      cudaStream_t st) {
     switch (cls) {
         case C_KIN: return launch_b<R, AX, C_KIN, P>(items, nitems, grid, smem, st);
         case C_EPI: return launch_b<R, AX, C_EPI, P>(items, nitems, grid, smem, st);
@@ -41,23 +51,15 @@ static cudaError_t launch_bc(int cls, const BatchItem<R>* items, int nitems, uns
         default: return launch_b<R, AX, C_EN, P>(items, nitems, grid, smem, st);
     }
 }
-
-template <typename R, int P>
-static cudaError_t launch_bp(int axis, int cls, const BatchItem<R>* items, int nitems, unsigned grid, size_t smem,
-                             cudaStream_t st) {
-    switch (axis) {
-        case AX_X: return launch_bc<R, AX_X, P>(cls, items, nitems, grid, smem, st);
-        case AX_Y: return launch_bc<R, AX_Y, P>(cls, items, nitems, grid, smem, st);
-        default: return launch_bc<R, AX_Z, P>(cls, items, nitems, grid, smem, st);
-    }
+#elif defined(GPE_BATCH_STUBS)
+template <typename R, int AX, int P>
+cudaError_t launch_bc(int, const BatchItem<R>*, int, unsigned, size_t, cudaStream_t) {
+    return cudaErrorInvalidValue;
 }
-
-template <>
-cudaError_t launch_batch<float>(int axis, int cls, int plan, const BatchItem<float>* items, int nitems,
-                                unsigned grid, size_t smem, cudaStream_t st) {
-    if (plan == 1) return launch_bp<float, 1>(axis, cls, items, nitems, grid, smem, st);
-    if (plan != 0) return cudaErrorInvalidValue;
-    return launch_bp<float, 0>(axis, cls, items, nitems, grid, smem, st);
-}
+#endif
 
 }  // namespace gpe
+
+#define GPE_INSTANTIATE_BATCH(AX, P)                                                                          \
+    template cudaError_t gpe::launch_bc<float, AX, P>(int, const gpe::BatchItem<float>*, int, unsigned, size_t, \
+                                                      cudaStream_t);

@@ -210,6 +210,7 @@ struct Engine {
     int sub = 1;        // internal sub-steps per step (the Weizsaecker term's stability bound)
     unsigned it = 0;
     double up[32] = {0};
+    double* d_up = nullptr;  // device copy of up (read by user hooks)
     cudaStream_t st = nullptr;
 
     void *psi = nullptr, *psi2 = nullptr, *lap = nullptr, *aux = nullptr, *V = nullptr, *Vqf = nullptr;
@@ -370,6 +371,7 @@ static int upload_tables(Engine* e) {
         e->ax[a].kk = dbase + okk;
     }
     GPE_CK(cudaMemcpyAsync(e->tabmem, host.data(), off, cudaMemcpyHostToDevice, e->st));
+    GPE_CK(cudaMemcpyAsync(e->d_up, e->up, sizeof e->up, cudaMemcpyHostToDevice, e->st));
     GPE_CK(cudaStreamSynchronize(e->st));
     e->graph_dirty = true;
     e->version++;
@@ -495,6 +497,8 @@ static PassArgs<R> base_args(const Engine* e) {
     a.lx = e->l3[0]; a.ly = e->l3[1]; a.lz = e->l3[2];
     a.npart = e->npart;
     a.dt = e->dt;
+    a.uparam = e->d_up;
+    a.t0 = e->t0;
     a.ph = make_phys<R>(e);
     return a;
 }
@@ -949,6 +953,7 @@ static void release(Engine* e) {
     cudaFree(e->dyn); cudaFree(e->partials); cudaFree(e->tabmem); cudaFree(e->stage); cudaFree(e->dens);
     cudaFree(e->vextra);
     cudaFree(e->phase);
+    cudaFree(e->d_up);
     if (e->st) cudaStreamDestroy(e->st);
 }
 
@@ -1479,6 +1484,10 @@ int gpe_gb_create(gpe_gb_engine** out, int nx, int ny, int nz, int interactions,
     *out = nullptr;
     if (!gpe::pow2_side(nx) || !gpe::pow2_side(ny) || !gpe::pow2_side(nz)) return GPE_ERR_LATTICE;
     if (interactions < -2 || interactions > 1) return GPE_ERR_FUNCTIONAL;
+#ifdef GPE_USER_HOOKS
+    // the hooks were compiled for one functional, which fixes Gamma
+    if (interactions != INTERACTIONS) return GPE_ERR_FUNCTIONAL;
+#endif
     if (precision != GPE_PRECISION_FP64 && precision != GPE_PRECISION_FP32) return GPE_ERR_ARGUMENT;
     gpe_gb_engine* h = new (std::nothrow) gpe_gb_engine();
     if (!h) return GPE_ERR_ARGUMENT;
@@ -1501,6 +1510,7 @@ int gpe_gb_create(gpe_gb_engine** out, int nx, int ny, int nz, int interactions,
     if (!rc && (ce = cudaMalloc(&e->aux, (precision == GPE_PRECISION_FP64 ? cs : rs) * e->n)) != cudaSuccess) rc = (int)ce;
     if (!rc && (ce = cudaMalloc(&e->V, rs * e->n)) != cudaSuccess) rc = (int)ce;
     if (!rc && (ce = cudaMalloc(&e->dyn, sizeof(gpe::DynState))) != cudaSuccess) rc = (int)ce;
+    if (!rc && (ce = cudaMalloc(&e->d_up, sizeof e->up)) != cudaSuccess) rc = (int)ce;
     if (!rc && (ce = cudaMalloc(&e->partials, sizeof(double) * gpe::NRED * gpe::max_grid(e))) != cudaSuccess) rc = (int)ce;
     if (!rc && (ce = cudaMemsetAsync(e->psi, 0, cs * e->n, e->st)) != cudaSuccess) rc = (int)ce;
     if (!rc && (ce = cudaMemsetAsync(e->dyn, 0, sizeof(gpe::DynState), e->st)) != cudaSuccess) rc = (int)ce;
@@ -1512,6 +1522,18 @@ int gpe_gb_create(gpe_gb_engine** out, int nx, int ny, int nz, int interactions,
         return rc;
     }
     *out = h;
+    return 0;
+}
+
+int gpe_gb_user_hooks(int* enabled, int* interactions) {
+    if (!enabled || !interactions) return GPE_ERR_ARGUMENT;
+#ifdef GPE_USER_HOOKS
+    *enabled = 1;
+    *interactions = INTERACTIONS;
+#else
+    *enabled = 0;
+    *interactions = 0;
+#endif
     return 0;
 }
 
@@ -1543,6 +1565,11 @@ int gpe_gb_set_time(gpe_gb_engine* h, double t0) {
     Engine* e = &h->e;
     e->t0 = t0;
     e->it = 0;
+#ifdef GPE_USER_HOOKS
+    // t0 is a launch argument of the captured steps (read by the hooks as d_t0)
+    e->graph_dirty = true;
+    e->version++;
+#endif
     // keep a pending ITE scale (none outside evolve) and reset the device step counter
     GPE_RC(gpe::set_state(e, 0, 1.0));
     return gpe::cuda_rc(cudaStreamSynchronize(e->st));
@@ -1619,6 +1646,12 @@ static int set_psi_from(Engine* e, double t, const void* src, cudaMemcpyKind kin
         e->launches++;
         GPE_CK(cudaGetLastError());
     }
+#ifdef GPE_USER_HOOKS
+    if (e->t0 != t) {  // t0 is a launch argument of the captured steps (read by the hooks as d_t0)
+        e->graph_dirty = true;
+        e->version++;
+    }
+#endif
     e->t0 = t;
     e->it = 0;
     e->lap_valid = false;
@@ -1974,6 +2007,12 @@ struct gpe_gb_control {
 
 int gpe_gb_control_create(gpe_gb_control** out, gpe_gb_engine* h, int nbasis, const double* basis, int nslices,
                           int steps_per_slice, int nsteps, int checkpoint_every, const double* psi_target) {
+#ifdef GPE_USER_HOOKS
+    // the adjoint restates the built-in contact-BEC step; user hooks have no adjoint here
+    (void)out; (void)h; (void)nbasis; (void)basis; (void)nslices; (void)steps_per_slice; (void)nsteps;
+    (void)checkpoint_every; (void)psi_target;
+    return GPE_ERR_NOT_IMPLEMENTED;
+#endif
     if (!out || !h || !basis || !psi_target) return GPE_ERR_ARGUMENT;
     *out = nullptr;
     Engine* e = &h->e;

@@ -119,6 +119,13 @@ cudaError_t launch_n(const PassArgs<R>& a, int axis, size_t pencils, cudaStream_
         default: return launch_ax<R, N, AX_Z, P>(a, pencils, st, g);
     }
 }
+#elif defined(GPE_PASS_STUBS)
+// A library built for a subset of pencil lengths (a hook library for tests): the lengths left out
+// refuse every pass over them.
+template <typename R, int N, int P>
+cudaError_t launch_n(const PassArgs<R>&, int, size_t, cudaStream_t, unsigned*) {
+    return cudaErrorInvalidValue;
+}
 #endif
 
 // Radix plan a pass over pencils of n points runs with when `plan` is requested: the alternative

@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "gpe_fft.cuh"
+#include "gpe_hooks.cuh"
 #include "gpe_physics.cuh"
 
 namespace gpe {
@@ -118,21 +119,52 @@ struct PassArgs {
     int lx, ly, lz;      // log2 of the lattice sides
     double npart, dt;
     int red_slot;
+    const double* uparam; // user parameters (device copy; read by user hooks)
+    double t0;            // initial time (user hooks)
     uint32_t npencils;   // pencils along this pass's axis
     uint32_t flags;
     int pre, mid, post;
     Phys<R> ph;
 };
 
+// External potential at step `it`: the built-in harmonic trap (per-axis tables), or the user hook
+// gpe_external_potential in a hook build; plus the time-sliced additive table when set.
 template <typename R> __device__ __forceinline__ R vext_at(const PassArgs<R>& a, uint32_t idx, int ix, int iy, int iz,
                                                           unsigned it) {
+#ifdef GPE_USER_HOOKS
+    R v = (R)gpe_external_potential((uint)ix, (uint)iy, (uint)iz, (uint)it);
+#else
     R v = (__ldg(a.vx + ix) + __ldg(a.vy + iy)) + __ldg(a.vz + iz);
+#endif
     if (a.flags & F_VEXTRA) {
         int s = (int)(it / (unsigned)a.vsteps);
         if (s >= a.vslices) s = a.vslices - 1;
         v += a.vextra[((size_t)s << (a.lx + a.ly + a.lz)) | idx];
     }
     return v;
+}
+
+// Mean field dE/drho at step `it`: built-in functional, or the user hook gpe_dEDFdn.
+template <typename R> __device__ __forceinline__ R mean_field(const PassArgs<R>& a, R rho, unsigned it) {
+#ifdef GPE_USER_HOOKS
+    (void)a;
+    return (R)gpe_dEDFdn((double)rho, (uint)it);
+#else
+    (void)it;
+    return dEDFdn(a.ph, rho);
+#endif
+}
+
+// psi_n as a step reads it: unchanged, or passed through the user hook gpe_modify_psi.
+template <typename R> __device__ __forceinline__ C2<R> modify_at(int ix, int iy, int iz, unsigned it, C2<R> v) {
+#ifdef GPE_USER_HOOKS
+    const cuDoubleComplex p = gpe_modify_psi((uint)ix, (uint)iy, (uint)iz, (uint)it,
+                                             make_cuDoubleComplex((double)v.x, (double)v.y));
+    return mk<R>((R)cuCreal(p), (R)cuCimag(p));
+#else
+    (void)ix; (void)iy; (void)iz; (void)it;
+    return v;
+#endif
 }
 
 template <typename C> __device__ __forceinline__ C ldc(const C* p) { return *p; }
@@ -487,6 +519,18 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
 #pragma unroll
         for (int q = 0; q < E; q++) x[q] = cscale(x[q], s_prev);
     }
+#ifdef GPE_USER_HOOKS
+    // run-time values the user hooks read (see gpe_hooks.cuh)
+    if (tid < 32) gpe_hook_ctx.up[tid] = a.uparam[tid];
+    if (tid == 0) {
+        gpe_hook_ctx.nx = 1u << a.lx;
+        gpe_hook_ctx.ny = 1u << a.ly;
+        gpe_hook_ctx.nz = 1u << a.lz;
+        gpe_hook_ctx.dt = a.dt;
+        gpe_hook_ctx.t0 = a.t0;
+        gpe_hook_ctx.npart = a.npart;
+    }
+#endif
     __syncthreads();  // tables staged
 
     double acc[NRED] = {0.0, 0.0, 0.0};
@@ -569,28 +613,33 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                 decode(idx, ix, iy, iz);
                 C2<R> v = own(q);
                 if (K == C_EPI && a.pre == PRE_VSTEP1) {
+                    v = modify_at<R>(ix, iy, iz, it, v);
                     const R rho = density(a.ph, v);
-                    const R V = vext_at(a, idx, ix, iy, iz, it) + dEDFdn(a.ph, rho);
+                    const R V = vext_at(a, idx, ix, iy, iz, it) + mean_field(a, rho, it);
                     a.V[idx] = V;
                     v = cmul(v, phase(a.ph, V));
                 } else if (K == C_EPI && a.pre == PRE_PART2) {
                     C2<R> p2 = a.psi2[idx];
                     if (a.flags & F_SCALE_PSI2) p2 = cscale(p2, s2);
                     const R rho = density(a.ph, p2);
-                    R lv = (a.V[idx] + vext_at(a, idx, ix, iy, iz, it + 1)) + dEDFdn(a.ph, rho);
+                    R lv = (a.V[idx] + vext_at(a, idx, ix, iy, iz, it + 1)) + mean_field(a, rho, it + 1);
                     if (a.flags & F_QF) lv += a.Vqf[idx];
                     lv = (R)0.5 * lv;
                     const C2<R> e = phase(a.ph, lv);
                     if (a.flags & F_AUX_CPLX) reinterpret_cast<C2<R>*>(a.aux)[idx] = e;
                     else reinterpret_cast<R*>(a.aux)[idx] = lv;
-                    v = cmul(v, e);
+                    v = cmul(modify_at<R>(ix, iy, iz, it, v), e);
                 } else if (K == C_EN && a.pre == PRE_ENERGY) {
                     const double px = (double)v.x, py = (double)v.y;
                     const double rho = (double)a.ph.gamma * (px * px + py * py);
                     Phys<double> phd;
                     phd.inter = a.ph.inter; phd.c_bec = (double)a.ph.c_bec; phd.a_scat = (double)a.ph.a_scat;
                     acc[0] += rho * (double)vext_at(a, idx, ix, iy, iz, it);
+#ifdef GPE_USER_HOOKS
+                    acc[1] += gpe_EDF(rho, (uint)it);
+#else
                     acc[1] += EDF(phd, rho);
+#endif
                 }
                 own(q) = v;
             }
@@ -628,12 +677,13 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                     const R vdip = own(q).x;  // real part of the convolution (dev/gpe_engine.cu:997-998)
                     C2<R> p = slotA[q * NT + tid];
                     if (sc) p = cscale(p, s_prev);
+                    if (dm == DIP_STEP) p = modify_at<R>(ix, iy, iz, it, p);
                     const R rho = density(a.ph, p);
                     if (dm == DIP_EN) {
                         acc[0] += 0.5 * (double)rho * (double)vdip;
                         own(q) = p;
                     } else {
-                        const R V = (vext_at(a, idx, ix, iy, iz, it) + dEDFdn(a.ph, rho)) + vdip;
+                        const R V = (vext_at(a, idx, ix, iy, iz, it) + mean_field(a, rho, it)) + vdip;
                         own(q) = cmul(p, phase(a.ph, V));
                     }
                 }
@@ -711,9 +761,17 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                         vqf += a.ph.wz8 * (slotC[q * NT + tid] * inv * inv - (R)2 * lrho * inv);
                     }
                     a.Vqf[idx] = vqf;
-                    const R V = (vext_at(a, idx, ix, iy, iz, it) + dEDFdn(a.ph, rho)) + vqf;
+                    // the gradient potential is taken from psi_n as stored; the step itself starts
+                    // from the (user-)modified psi_n (dev/gpe_engine.cu:1040-1041, 758-760)
+                    const C2<R> pm = modify_at<R>(ix, iy, iz, it, p);
+#ifdef GPE_USER_HOOKS
+                    const R rho_m = density(a.ph, pm);
+#else
+                    const R rho_m = rho;
+#endif
+                    const R V = (vext_at(a, idx, ix, iy, iz, it) + mean_field(a, rho_m, it)) + vqf;
                     a.V[idx] = V;
-                    own(q) = cmul(p, phase(a.ph, V));
+                    own(q) = cmul(pm, phase(a.ph, V));
                 }
                 from_cells();
             } else if (a.mid == MID_CURRENT) {
@@ -753,7 +811,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                     R lv = op_v(q, idx);
                     const C2<R> pp = cmul(v, phase(a.ph, lv));
                     const R rho = density(a.ph, pp);
-                    lv = (lv + vext_at(a, idx, ix, iy, iz, it + 1)) + dEDFdn(a.ph, rho);
+                    lv = (lv + vext_at(a, idx, ix, iy, iz, it + 1)) + mean_field(a, rho, it + 1);
                     if (a.post == POST_PART12 && (a.flags & F_QF)) lv += op_vqf(q, idx);
                     lv = (R)0.5 * lv;
                     const C2<R> e = phase(a.ph, lv);
@@ -761,7 +819,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                     else reinterpret_cast<R*>(a.aux)[idx] = lv;
                     C2<R> p = op_psi(q, idx);
                     if (scale_in) p = cscale(p, s_prev);
-                    v = cmul(p, e);
+                    v = cmul(modify_at<R>(ix, iy, iz, it, p), e);
                 } else if (a.post == POST_PART1) {
                     v = cmul(v, phase(a.ph, op_v(q, idx)));
                 } else if (a.post == POST_VSTEP3) {

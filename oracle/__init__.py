@@ -84,8 +84,43 @@ def lib():
         L.oracle_set_phase.argtypes = [vp, dp]
         L.oracle_evolve_enforced.argtypes = [vp, i, dp, i]
         L.oracle_evolve_enforced.restype = i
+        L.oracle_set_hooks.argtypes = [vp, vp, vp, vp, vp]
         _lib = L
     return _lib
+
+
+def build_hooks(header: str, name: str, defines=()) -> str:
+    """Compiles a user hook header for the host (oracle/hooks_host.cpp) into
+    oracle/_build/libhooks_<name>.so, so that the oracle evaluates the same hooks as a hook build of
+    the engine.  `defines`: preprocessor definitions ("VEXT=1", "INTERACTIONS=-1", ...)."""
+    os.makedirs(BUILD, exist_ok=True)
+    header = os.path.abspath(header)
+    out = os.path.join(BUILD, f"libhooks_{name}.so")
+    src = os.path.join(HERE, "hooks_host.cpp")
+    tmp = out + f".tmp{os.getpid()}"
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-I", "/usr/local/cuda/include",
+           f'-DGPE_USER_HOOKS="{header}"', *[f"-D{d}" for d in defines], src, "-o", tmp, "-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, out)
+    return out
+
+
+class Hooks:
+    """A host build of a user hook header (build_hooks), handed to Oracle.set_hooks."""
+
+    def __init__(self, path: str):
+        self.path = path
+        self.L = ctypes.CDLL(path)
+        self.L.hooks_set.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_uint, ctypes.c_uint,
+                                     ctypes.c_uint, ctypes.c_double, ctypes.c_double, ctypes.c_double]
+        self.L.hooks_interactions.restype = ctypes.c_int
+
+    def address(self, name: str) -> int:
+        return ctypes.cast(getattr(self.L, name), ctypes.c_void_p).value
+
+    @property
+    def interactions(self) -> int:
+        return self.L.hooks_interactions()
 
 
 def _dp(a: np.ndarray):
@@ -105,6 +140,24 @@ class Oracle:
             raise ValueError(f"unsupported lattice {shape}")
         L.oracle_set_threads(self._h, int(threads))
         self._vextra = None
+        self._hooks = None
+        self._params = np.zeros(0)
+        self._t0 = 0.0
+        self._dt, self._npart = float(dt), float(npart)
+
+    def set_hooks(self, hooks: "Hooks"):
+        """Evaluate the user hooks of `hooks` instead of the built-in trap and functional (the hook
+        library holds one set of run-time values: one oracle per hook library at a time)."""
+        self._hooks = hooks
+        lib().oracle_set_hooks(self._h, hooks.address("hooks_vext"), hooks.address("hooks_dedf"),
+                               hooks.address("hooks_edf"), hooks.address("hooks_modify"))
+        self._push_hook_values()
+
+    def _push_hook_values(self):
+        if self._hooks is not None:
+            p = np.ascontiguousarray(self._params, dtype=np.float64)
+            self._hooks.L.hooks_set(_dp(p), len(p), *[ctypes.c_uint(s) for s in self.shape], self._dt, self._t0,
+                                    self._npart)
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -117,12 +170,16 @@ class Oracle:
 
     def set_user_params(self, params):
         p = np.ascontiguousarray(params, dtype=np.float64)
+        self._params = p.copy()
+        self._push_hook_values()
         return lib().oracle_set_user_params(self._h, len(p), _dp(p))
 
     def change_alpha_beta(self, alpha, beta):
         lib().oracle_change_alpha_beta(self._h, float(alpha), float(beta))
 
     def set_time(self, t0):
+        self._t0 = float(t0)
+        self._push_hook_values()
         lib().oracle_set_time(self._h, float(t0))
 
     def set_quantum_friction_coeff(self, q):
@@ -133,6 +190,8 @@ class Oracle:
         lib().oracle_set_vextra(self._h, _dp(self._vextra), self._vextra.shape[0], int(steps_per_slice))
 
     def set_psi(self, t, psi):
+        self._t0 = float(t)
+        self._push_hook_values()
         p = np.ascontiguousarray(psi, dtype=np.complex128).reshape(self.shape)
         lib().oracle_set_psi(self._h, float(t), _dp(p.view(np.float64)))
 

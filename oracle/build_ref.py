@@ -104,12 +104,14 @@ def prepare() -> bool:
     return True
 
 
-def binary_name(nx: int, ny: int, nz: int, inter: int) -> str:
-    return os.path.join(BIN, f"ref_{nx}x{ny}x{nz}_i{inter}")
+def binary_name(nx: int, ny: int, nz: int, inter: int, vext: int = 0) -> str:
+    return os.path.join(BIN, f"ref_{nx}x{ny}x{nz}_i{inter}" + (f"_v{vext}" if vext else ""))
 
 
-def build_one(nx: int, ny: int, nz: int, inter: int, arch: str = "103a") -> str:
-    out = binary_name(nx, ny, nz, inter)
+def build_one(nx: int, ny: int, nz: int, inter: int, arch: str = "103a", vext: int = 0) -> str:
+    """One reference binary for this lattice and functional; `vext` selects the reference's external
+    potential (0 harmonic trap, 1 Woods-Saxon tube: dev/gpe_user_defined.h:478-558)."""
+    out = binary_name(nx, ny, nz, inter, vext)
     runner = os.path.join(HERE, "ref_runner.cpp")
     srcs = [os.path.join(SRC, "gpe_engine.cu"), os.path.join(SRC, "reductions.cu"), runner]
     if os.path.isfile(out) and all(os.path.getmtime(out) > os.path.getmtime(s) for s in srcs):
@@ -118,7 +120,7 @@ def build_one(nx: int, ny: int, nz: int, inter: int, arch: str = "103a") -> str:
     tmp = out + f".tmp{os.getpid()}"
     cmd = ["nvcc", "-O3", "-rdc=true", f"-gencode=arch=compute_{arch},code=sm_{arch}",
            "-w", "-include", os.path.join(SRC, "cufft_compat.h"), "-I", SRC,
-           f"-DNX={nx}", f"-DNY={ny}", f"-DNZ={nz}", f"-DINTERACTIONS={inter}", "-DVEXT=0",
+           f"-DNX={nx}", f"-DNY={ny}", f"-DNZ={nz}", f"-DINTERACTIONS={inter}", f"-DVEXT={vext}",
            *srcs, "-lcufft", "-o", tmp]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -57,6 +57,11 @@ static inline cd cmul(cd a, cd b) { cd c; c.x = a.x * b.x - a.y * b.y; c.y = a.x
 static inline cd cscale(cd a, double s) { cd c; c.x = s * a.x; c.y = s * a.y; return c; }
 static inline cd cexp_(cd z) { double t = exp(z.x); cd r; r.x = t * cos(z.y); r.y = t * sin(z.y); return r; }
 
+/* user hooks (a hook header compiled for the host by oracle/hooks_host.cpp); NULL = built-in physics */
+typedef double (*orc_vext_fn)(unsigned ix, unsigned iy, unsigned iz, unsigned it);
+typedef double (*orc_rho_fn)(double rho, unsigned it);
+typedef void (*orc_modify_fn)(unsigned ix, unsigned iy, unsigned iz, unsigned it, double *re, double *im);
+
 typedef struct {
     int nx, ny, nz;
     size_t n;
@@ -85,6 +90,11 @@ typedef struct {
     int sub;              /* sub-steps per step while the Weizsaecker term is on */
     cd *wz1;
     double *wzG, *wzS;
+    /* user hooks (dev/gpe_user_defined.h names: gpe_external_potential, gpe_dEDFdn, gpe_EDF,
+     * gpe_modify_psi) */
+    orc_vext_fn hk_vext;
+    orc_rho_fn hk_dedf, hk_edf;
+    orc_modify_fn hk_modify;
 } gpe_oracle;
 
 /* ---------------------------------------------------------------- helpers */
@@ -193,12 +203,17 @@ static void fft3d(const gpe_oracle *o, cd *a, int sign) {
 static inline double density(const gpe_oracle *o, cd p) { return o->gamma * (p.x * p.x + p.y * p.y); }
 
 static inline double vext(const gpe_oracle *o, size_t idx, int ix, int iy, int iz, unsigned it) {
-    /* dev/gpe_user_defined.h:488-513 */
-    const double wx = o->up[0], wy = o->up[1], wz = o->up[2];
-    const double _ix = (double)ix - 1.0 * (o->nx / 2);
-    const double _iy = (double)iy - 1.0 * (o->ny / 2);
-    const double _iz = (double)iz - 1.0 * (o->nz / 2);
-    double v = 0.5 * _ix * _ix * wx * wx + 0.5 * _iy * _iy * wy * wy + 0.5 * _iz * _iz * wz * wz;
+    /* dev/gpe_user_defined.h:488-513, or the user hook gpe_external_potential */
+    double v;
+    if (o->hk_vext) {
+        v = o->hk_vext((unsigned)ix, (unsigned)iy, (unsigned)iz, it);
+    } else {
+        const double wx = o->up[0], wy = o->up[1], wz = o->up[2];
+        const double _ix = (double)ix - 1.0 * (o->nx / 2);
+        const double _iy = (double)iy - 1.0 * (o->ny / 2);
+        const double _iz = (double)iz - 1.0 * (o->nz / 2);
+        v = 0.5 * _ix * _ix * wx * wx + 0.5 * _iy * _iy * wy * wy + 0.5 * _iz * _iz * wz * wz;
+    }
     if (o->vextra) {
         int s = (int)(it / ((unsigned)o->steps_per_slice * (unsigned)o->sub));
         if (s >= o->nslices) s = o->nslices - 1;
@@ -210,7 +225,25 @@ static inline double vext(const gpe_oracle *o, size_t idx, int ix, int iy, int i
 #define ORC_XI 0.37
 #define ORC_CONTACT 0.901
 
-static inline double dEDFdn(const gpe_oracle *o, double rho) {
+/* psi as a step reads it: the user hook gpe_modify_psi (dev/gpe_user_defined.h:81-85), called at
+ * dev/gpe_engine.cu:733, 758, 794, 834, 861, 999 */
+static inline cd modify(const gpe_oracle *o, int ix, int iy, int iz, unsigned it, cd p) {
+    if (o->hk_modify) o->hk_modify((unsigned)ix, (unsigned)iy, (unsigned)iz, it, &p.x, &p.y);
+    return p;
+}
+
+static inline double dEDFdn_builtin(const gpe_oracle *o, double rho);
+static inline double EDF_builtin(const gpe_oracle *o, double rho);
+
+/* functional at step `it`: the user hooks gpe_dEDFdn / gpe_EDF, or the built-in ones */
+static inline double dEDFdn(const gpe_oracle *o, double rho, unsigned it) {
+    return o->hk_dedf ? o->hk_dedf(rho, it) : dEDFdn_builtin(o, rho);
+}
+static inline double EDF(const gpe_oracle *o, double rho, unsigned it) {
+    return o->hk_edf ? o->hk_edf(rho, it) : EDF_builtin(o, rho);
+}
+
+static inline double dEDFdn_builtin(const gpe_oracle *o, double rho) {
     if (o->inter == 0) return 0.37 * pow(3.0 * M_PI * M_PI * rho, 2.0 / 3.0) / 2.0;
     if (o->inter == -1) { const double a = o->up[3]; return 4 * M_PI * a * rho; }
     if (o->inter == -2) return 0.0; /* dipolar BEC: dev/gpe_user_defined.h:400-404 */
@@ -230,7 +263,7 @@ static inline double dEDFdn(const gpe_oracle *o, double rho) {
     return 0.0;
 }
 
-static inline double EDF(const gpe_oracle *o, double rho) {
+static inline double EDF_builtin(const gpe_oracle *o, double rho) {
     if (o->inter == 0) return 0.37 * 0.6 * rho * pow(3.0 * M_PI * M_PI * rho, 2.0 / 3.0) / 2.;
     if (o->inter == -1 || o->inter == -2) { const double a = o->up[3]; return 2 * M_PI * a * rho * rho; }
     if (o->inter == 1) {
@@ -326,6 +359,14 @@ void oracle_change_alpha_beta(void *h, double alpha, double beta) {
     gpe_oracle *o = (gpe_oracle *)h;
     o->alpha = alpha; o->beta = beta;
     tables(o);
+}
+
+void oracle_set_hooks(void *h, void *vext_fn, void *dedf_fn, void *edf_fn, void *modify_fn) {
+    gpe_oracle *o = (gpe_oracle *)h;
+    o->hk_vext = (orc_vext_fn)vext_fn;
+    o->hk_dedf = (orc_rho_fn)dedf_fn;
+    o->hk_edf = (orc_rho_fn)edf_fn;
+    o->hk_modify = (orc_modify_fn)modify_fn;
 }
 
 void oracle_set_time(void *h, double t0) { gpe_oracle *o = (gpe_oracle *)h; o->t0 = t0; o->it = 0; }
@@ -593,9 +634,9 @@ static int evolve_impl(gpe_oracle *o, int nt, double *mu, int mode, int mid_repe
 #pragma omp parallel for num_threads(o->nthreads) schedule(static)
         for (long i = 0; i < n; i++) {
             DECODE((size_t)i);
-            const cd lpsi = o->psi[i];
+            const cd lpsi = modify(o, ix, iy, iz, it, o->psi[i]);
             const double lrho = density(o, lpsi);
-            double lv = vext(o, (size_t)i, ix, iy, iz, it) + dEDFdn(o, lrho);
+            double lv = vext(o, (size_t)i, ix, iy, iz, it) + dEDFdn(o, lrho, it);
             if (qf) lv += o->Vqf[i];
             o->V[i] = lv;
             o->psi2[i] = cmul(lpsi, cexp_(cscale(o->c3, lv)));
@@ -612,10 +653,10 @@ static int evolve_impl(gpe_oracle *o, int nt, double *mu, int mode, int mid_repe
                 double lv = o->V[i];
                 cd lpsi = cmul(o->psi2[i], cexp_(cscale(o->c3, lv)));
                 const double lrho = density(o, lpsi);
-                lv = 0.5 * (lv + vext(o, (size_t)i, ix, iy, iz, it + 1) + dEDFdn(o, lrho));
+                lv = 0.5 * (lv + vext(o, (size_t)i, ix, iy, iz, it + 1) + dEDFdn(o, lrho, it + 1));
                 const cd e = cexp_(cscale(o->c3, lv));
                 o->wrkC[i] = e;
-                o->psi[i] = cmul(o->psi[i], e);
+                o->psi[i] = cmul(modify(o, ix, iy, iz, it, o->psi[i]), e);
             }
         } else {
             /* part1: dev/gpe_engine.cu:799-811 */
@@ -631,12 +672,12 @@ static int evolve_impl(gpe_oracle *o, int nt, double *mu, int mode, int mid_repe
             for (long i = 0; i < n; i++) {
                 DECODE((size_t)i);
                 const double lrho = density(o, o->psi2[i]);
-                double lv = o->V[i] + vext(o, (size_t)i, ix, iy, iz, it + 1) + dEDFdn(o, lrho);
+                double lv = o->V[i] + vext(o, (size_t)i, ix, iy, iz, it + 1) + dEDFdn(o, lrho, it + 1);
                 if (qf) lv += o->Vqf[i];
                 lv = 0.5 * lv;
                 const cd e = cexp_(cscale(o->c3, lv));
                 o->wrkC[i] = e;
-                o->psi[i] = cmul(o->psi[i], e);
+                o->psi[i] = cmul(modify(o, ix, iy, iz, it, o->psi[i]), e);
             }
         }
         fft3d(o, o->psi, -1);
@@ -667,7 +708,7 @@ int oracle_energy(void *h, double *t, double *ekin, double *eint, double *eext) 
         DECODE((size_t)i);
         const double lrho = density(o, o->psi[i]);
         w1[i] = lrho * vext(o, (size_t)i, ix, iy, iz, o->it);
-        w2[i] = EDF(o, lrho);
+        w2[i] = EDF(o, lrho, o->it);
     }
     *eext = det_sum(o, w1);
     *eint = det_sum(o, w2);
@@ -746,9 +787,9 @@ static void dipolar_vstep(gpe_oracle *o, unsigned it) {
 #pragma omp parallel for num_threads(o->nthreads) schedule(static)
     for (long i = 0; i < n; i++) {
         DECODE((size_t)i);
-        const cd lpsi = o->psi[i];
+        const cd lpsi = modify(o, ix, iy, iz, it, o->psi[i]);
         const double lrho = density(o, lpsi);
-        const double lv = vext(o, (size_t)i, ix, iy, iz, it) + dEDFdn(o, lrho) + o->V[i];
+        const double lv = vext(o, (size_t)i, ix, iy, iz, it) + dEDFdn(o, lrho, it) + o->V[i];
         o->psi[i] = cmul(lpsi, cexp_(cscale(o->c3, lv)));
     }
 }

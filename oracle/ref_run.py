@@ -18,14 +18,14 @@ def available() -> bool:
     return build_ref.prepare()
 
 
-def run(shape, interactions, alpha, beta, dt, npart, params, psi0, cmds, qf=0.0, timeout=600):
+def run(shape, interactions, alpha, beta, dt, npart, params, psi0, cmds, qf=0.0, timeout=600, vext=0):
     """Executes `cmds` (see oracle/ref_runner.cpp) and returns the parsed results.
 
     Returns dict with 'psi' (list of dumps), 'energy' (list of (t, ekin, eint, eext)),
     'mu' (list), 'time_ms' (list).
     """
     nx, ny, nz = shape
-    exe = build_ref.build_one(nx, ny, nz, interactions)
+    exe = build_ref.build_one(nx, ny, nz, interactions, vext=vext)
     p = list(params) + [0.0] * (4 - len(params))
     with tempfile.TemporaryDirectory() as d:
         inp = os.path.join(d, "psi0.bin")
