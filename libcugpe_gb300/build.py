@@ -130,7 +130,7 @@ def build(jobs: int | None = None, verbose: bool = False, hooks: str | None = No
     os.makedirs(build_dir, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     extra = [f"-D{d}" for d in defines]
-    deps = _headers() + [__file__]
+    deps = _headers() + [__file__, os.path.join(CSRC, "exports.map")]
     if hooks:
         hooks = os.path.abspath(hooks)
         if not os.path.isfile(hooks):
@@ -149,7 +149,8 @@ def build(jobs: int | None = None, verbose: bool = False, hooks: str | None = No
     if os.path.isfile(lib) and os.path.getmtime(lib) > max(os.path.getmtime(o) for o in objs):
         return lib
     tmp = lib + f".tmp{os.getpid()}"
-    cmd = ["nvcc", *ARCH, "-shared", "-Xcompiler", "-fPIC", *objs, "-o", tmp, "-lcudart"]
+    cmd = ["nvcc", *ARCH, "-shared", "-Xcompiler", "-fPIC", *objs, "-o", tmp, "-lcudart",
+           "-Xlinker", "--version-script=" + os.path.join(CSRC, "exports.map")]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stderr[-6000:]}")

@@ -422,7 +422,10 @@ static std::vector<PassDesc> schedule(const Engine* e, bool first) {
     std::vector<PassDesc> s;
     const bool ite = e->beta != 0.0;
     const bool qf = e->grad_terms();
-    const uint32_t aux = (e->prec == GPE_PRECISION_FP64) ? F_AUX_CPLX : 0u;
+    // corrector factor stored as complex exp(c3 V') (Vstep3 then needs no sincos) where the extra 4 bytes
+    // per point stay in L2 (FP32 lattices of <= 2^21 points) and always in FP64 (ALU-bound); else the
+    // real V' (FP32 on HBM-resident lattices: recomputing the phase is cheaper than moving 4 more bytes)
+    const uint32_t aux = (e->prec == GPE_PRECISION_FP64 || e->n <= ((size_t)1 << 21)) ? F_AUX_CPLX : 0u;
     const uint32_t sin_ = ite ? F_SCALE_IN : 0u;
     if (!qf) {
         s.push_back({AX_Z, PRE_VSTEP1, MID_NONE, POST_NONE, F_KIN | F_STORE | sin_, B_PSI, B_PSI2});
@@ -1507,7 +1510,9 @@ int gpe_gb_create(gpe_gb_engine** out, int nx, int ny, int nz, int interactions,
     if ((ce = cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking)) != cudaSuccess) rc = (int)ce;
     if (!rc && (ce = cudaMalloc(&e->psi, cs * e->n)) != cudaSuccess) rc = (int)ce;
     if (!rc && (ce = cudaMalloc(&e->psi2, cs * e->n)) != cudaSuccess) rc = (int)ce;
-    if (!rc && (ce = cudaMalloc(&e->aux, (precision == GPE_PRECISION_FP64 ? cs : rs) * e->n)) != cudaSuccess) rc = (int)ce;
+    if (!rc && (ce = cudaMalloc(&e->aux, (precision == GPE_PRECISION_FP64 || e->n <= ((size_t)1 << 21) ? cs : rs) *
+                                          e->n)) != cudaSuccess)
+        rc = (int)ce;
     if (!rc && (ce = cudaMalloc(&e->V, rs * e->n)) != cudaSuccess) rc = (int)ce;
     if (!rc && (ce = cudaMalloc(&e->dyn, sizeof(gpe::DynState))) != cudaSuccess) rc = (int)ce;
     if (!rc && (ce = cudaMalloc(&e->d_up, sizeof e->up)) != cudaSuccess) rc = (int)ce;

@@ -243,20 +243,20 @@ template <typename R, int NT, int NR>
 __device__ void finalize(const PassArgs<R>& a, double (*sred)[NRED], uint32_t nblk, bool sums) {
     double s[NRED] = {0.0, 0.0, 0.0};
     if (sums) {
-        double s2[NRED] = {0.0, 0.0, 0.0};  // two chains per value
-        int b = threadIdx.x;
-        for (; b + NT < (int)nblk; b += 2 * NT) {
+        // each thread sums its partials (a fixed stride) with Neumaier's compensation, then the
+        // block adds the compensated per-thread sums in a fixed order
+        double c[NRED] = {0.0, 0.0, 0.0};
+        for (int b = threadIdx.x; b < (int)nblk; b += NT) {
 #pragma unroll
             for (int r = 0; r < NR; r++) {
-                s[r] += __ldcg(a.partials + (size_t)b * NRED + r);
-                s2[r] += __ldcg(a.partials + (size_t)(b + NT) * NRED + r);
+                const double x = __ldcg(a.partials + (size_t)b * NRED + r);
+                const double t = s[r] + x;
+                c[r] += (fabs(s[r]) >= fabs(x)) ? (s[r] - t) + x : (x - t) + s[r];
+                s[r] = t;
             }
         }
-        if (b < (int)nblk)
 #pragma unroll
-            for (int r = 0; r < NR; r++) s[r] += __ldcg(a.partials + (size_t)b * NRED + r);
-#pragma unroll
-        for (int r = 0; r < NR; r++) s[r] += s2[r];
+        for (int r = 0; r < NR; r++) s[r] += c[r];
         block_sum<NT, NR>(s, sred);
     }
     if (threadIdx.x == 0) {
@@ -310,7 +310,7 @@ __host__ __device__ inline uint32_t staged_ops(int mid, int post, uint32_t flags
     if (post == POST_PART12 && (flags & F_QF)) m |= OP_VQF;
     if (post == POST_PART1) m |= OP_V;
     if (post == POST_VSTEP3) m |= (flags & F_AUX_CPLX) ? OP_AUXC : OP_AUXR;
-    if (flags & F_DIRECT) m &= ~(OP_PSI | OP_V | OP_VQF | OP_LAP | OP_COPY);
+    if (flags & F_DIRECT) m &= ~(OP_PSI | OP_V | OP_VQF | OP_LAP | OP_COPY | OP_AUXC);
     return m;
 }
 
@@ -425,11 +425,11 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     __shared__ bool last_cta;
 
     // Programmatic dependent launch: the FP32 pass kernels are launched so that their CTAs may start
-    // while the previous pass drains; every global read below comes after the wait for that pass
-    // to complete (a no-op for a launch without the attribute).  Dependents may be launched as
-    // soon as every CTA of this pass is running.
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    // while the previous pass drains.  The constant tables (written before any pass of the stream
+    // ran) are staged first, overlapping that drain; every read of what earlier passes wrote (psi,
+    // operands, the device state) comes after the wait for the previous pass to complete (a no-op
+    // for a launch without the attribute).  Dependents may be launched as soon as every CTA of this
+    // pass is running.
     const int tid = threadIdx.x;
     for (int i = tid; i < Geo::TW; i += NT) stw[i] = a.tw[i];
     if constexpr (K != C_EN) {
@@ -438,6 +438,8 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     if constexpr (K != C_KIN) {
         for (int i = tid; i < N; i += NT) slt[i] = a.ltab[i];
     }
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 
     int pl, t, bar;
     C2<R>* sb;
@@ -824,7 +826,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                     v = cmul(v, phase(a.ph, op_v(q, idx)));
                 } else if (a.post == POST_VSTEP3) {
                     C2<R> e;
-                    if (a.flags & F_AUX_CPLX) e = slotA[q * NT + tid];
+                    if (a.flags & F_AUX_CPLX) e = direct ? reinterpret_cast<const C2<R>*>(a.aux)[idx] : slotA[q * NT + tid];
                     else e = phase(a.ph, slotC[q * NT + tid]);
                     v = cmul(v, e);
                 }
@@ -908,15 +910,16 @@ __device__ __forceinline__ void kin_pipe_body(const PassArgs<R>& a) {
     constexpr int E = Geo::E, T = Geo::T, CW = Geo::CW, G = Geo::G, W = Geo::W, ROW = Geo::ROW;
     constexpr int SSTR = (AX == AX_Z) ? 1 : CW;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     C2<R>* stw = reinterpret_cast<C2<R>*>(smem_raw);
     C2<R>* skt = stw + Geo::TW;
     C2<R>* sx = reinterpret_cast<C2<R>*>(smem_raw + Geo::TAB_BYTES);
     C2<R>* stg = reinterpret_cast<C2<R>*>(smem_raw + Geo::SMEM_BASE);
     const int tid = threadIdx.x;
+    // constant tables first (they overlap the previous pass's drain), then wait for that pass
     for (int i = tid; i < Geo::TW; i += NT) stw[i] = a.tw[i];
     for (int i = tid; i < N; i += NT) skt[i] = a.ktab[i];
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     int pl, t, bar;
     C2<R>* sb;
     if constexpr (AX == AX_Z) {
