@@ -136,6 +136,11 @@ int gpe_gb_use_graphs(gpe_gb_engine* e, int enable);
  * nx*ny*nz doubles; step `it` uses slice min(it / steps_per_slice, nslices-1)
  * on top of the harmonic trap.  NULL removes it. */
 int gpe_gb_set_potential_slices(gpe_gb_engine* e, const double* fields, int nslices, int steps_per_slice);
+/* Pass layout of the step (no reference counterpart): enable = 1 (default) runs
+ * real-time FP32 steps on 128 x 128 yz-planes as four launches (two yz-plane
+ * passes, two x-pencil passes), enable = 0 keeps the seven pencil passes.
+ * Both compute the same step (FP32 rounding apart). */
+int gpe_gb_set_plane_passes(gpe_gb_engine* e, int enable);
 /* Whether this library was built with a user hook header (include/gpe_user_defined.h;
  * no reference counterpart: the reference recompiles instead): *enabled = 1 and
  * *interactions = the functional the hooks were compiled for (gpe_gb_create

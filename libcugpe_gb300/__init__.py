@@ -51,7 +51,7 @@ C_ABI_SYMBOLS = [
     "gpe_gb_snapshots_close", "gpe_gb_dftc_write_info", "gpe_gb_dftc_read_info", "gpe_gb_set_weizsacker",
     "gpe_gb_evolve_dipolar", "gpe_gb_energy_dipolar", "gpe_gb_autotune", "gpe_gb_batch_autotune",
     "gpe_gb_set_fft_plan", "gpe_gb_get_fft_plan", "gpe_gb_batch_set_fft_plan", "gpe_gb_fp64_fma_rate",
-    "gpe_gb_user_hooks",
+    "gpe_gb_user_hooks", "gpe_gb_set_plane_passes",
 ]
 
 
@@ -112,6 +112,7 @@ def _lib(path: str | None = None):
             "gpe_gb_norm_noalloc": (i, [vp, i, ctypes.c_longlong, d, vp, vp]),
             "gpe_gb_fp64_fma_rate": (i, [dp]),
             "gpe_gb_user_hooks": (i, [ip, ip]),
+            "gpe_gb_set_plane_passes": (i, [vp, i]),
             "gpe_gb_set_vortex": (i, [vp, d, d, i]),
             "gpe_gb_get_phase": (i, [vp, dp]),
             "gpe_gb_set_phase": (i, [vp, dp]),
@@ -289,6 +290,10 @@ class Engine:
                                       ctypes.byref(ms)), "autotune")
         return {"direct": d.value, "graph_steps": c.value, "fft_plan": p.value, "ms_per_step": ms.value}
 
+    def set_plane_passes(self, enable: bool):
+        """Real-time FP32 steps on 128 x 128 yz-planes as yz-plane passes (default) or pencil passes only."""
+        _check(self._L.gpe_gb_set_plane_passes(self._h, 1 if enable else 0), "set_plane_passes", self._L)
+
     def set_fft_plan(self, plan):
         """Radix plan of the pencil FFTs: 0 default, 1 the alternative (FP32, pencils of 32-512 points)."""
         _check(self._L.gpe_gb_set_fft_plan(self._h, int(plan)), "set_fft_plan", self._L)
@@ -363,7 +368,8 @@ class Engine:
         npass = ctypes.c_int()
         _check(self._L.gpe_gb_profile_passes(self._h, int(nsteps), ms, by, ax, kd, cap, ctypes.byref(npass)),
                "profile_passes")
-        return [{"ms": ms[p], "bytes": by[p], "axis": "xyz"[ax[p]], "kind": ("kin", "epi", "lap", "energy")[kd[p]]}
+        kinds = {0: "kin", 1: "epi", 2: "lap", 3: "energy", 4: "dipolar", 8: "plane"}
+        return [{"ms": ms[p], "bytes": by[p], "axis": ("x", "y", "z", "yz")[ax[p]], "kind": kinds.get(kd[p], str(kd[p]))}
                 for p in range(min(npass.value, cap))]
 
     def use_graphs(self, enable: bool):

@@ -77,8 +77,8 @@ def _sources(build_dir, lengths, precisions, batch=True):
         _write_if_changed(path, '#define GPE_BATCH_STUBS\n#include "gpe_batch_kernels.cuh"\n' + "".join(
             f"GPE_INSTANTIATE_BATCH(gpe::AX_{ax}, {plan})\n" for ax in ("X", "Y", "Z") for plan in (0, 1)))
         units.append(path)
-    for f in ("gpe_engine.cu", "gpe_noalloc.cu", "gpe_probe.cu", "gpe_batch_dispatch.cu", "gpe_dropin.cpp",
-              "gpe_snapshots.cpp"):
+    for f in ("gpe_engine.cu", "gpe_plane.cu", "gpe_noalloc.cu", "gpe_probe.cu", "gpe_batch_dispatch.cu",
+              "gpe_dropin.cpp", "gpe_snapshots.cpp"):
         units.append(os.path.join(CSRC, f))
     return units
 

@@ -33,6 +33,7 @@
 #include <vector>
 
 #include "gpe_launch.cuh"
+#include "gpe_plane.cuh"
 #include "gpe_batch.cuh"
 #include "../../include/gpe_gb300.h"
 
@@ -232,6 +233,7 @@ struct Engine {
     int direct_mode = -1;   // operands read where used: -1 by lattice size, 0 staged, 1 direct (autotuner)
     int graph_chunk = 16;   // steps per replayed graph (autotuner)
     int fft_plan = 0;       // radix plan of the pencil FFTs: 0 default, 1 alternative (FP32; autotuner)
+    int plane_mode = -1;    // yz-plane passes: -1 where supported, 0 pencil passes only
     // radix plan per fused pass of the steady schedule, chosen by the autotuner from per-pass timings
     // (key: pass_key); passes without an entry run fft_plan
     std::vector<std::pair<uint64_t, int>> pass_plan;
@@ -403,6 +405,11 @@ static Phys<R> make_phys(const Engine* e) {
     return p;
 }
 
+cudaError_t launch_plane(const PlaneArgs& pa, int n, unsigned planes, cudaStream_t st);
+
+// Pass axis of the yz-plane pass (gpe_plane.cuh): one launch covers the y and z transforms.
+constexpr int AX_YZ = 3;
+
 struct PassDesc {
     int axis;
     int pre, mid, post;
@@ -417,11 +424,39 @@ static uint64_t pass_key(const PassDesc& d) {
            ((uint64_t)(d.mid & 0xff) << 8) | (uint64_t)(d.post & 0xff);
 }
 
+// Whether a step of this engine can run as yz-plane passes (gpe_plane.cuh): FP32 real time on square
+// 128 x 128 planes, without the Weizsaecker term.
+static bool plane_schedule(const Engine* e) {
+    return e->plane_mode != 0 && e->prec == GPE_PRECISION_FP32 && e->beta == 0.0 && e->wz == 0.0 &&
+           e->n3[1] == 128 && e->n3[2] == 128;
+}
+
 // The reference step sequence (dev/gpe_engine.cu:1035-1106) as fused passes.
-static std::vector<PassDesc> schedule(const Engine* e, bool first) {
+// With yz-plane passes (real time, FP32): the kinetic sub-steps are K_x then K_y K_z in one plane pass,
+//   friction: x: D_x psi + lap -> V_qf, Vstep1_qf, K_x -> psi2;  yz: K_y K_z, corrector -> psi;
+//             x: K_x;  yz: K_y K_z, Vstep3 -> psi, then (D_y + D_z) psi -> lap for the next step
+//   plain:    yz: Vstep1, K_y K_z -> psi2;  x: K_x, Vstep2 -> psi;  yz: K_y K_z;  x: K_x, Vstep3
+static std::vector<PassDesc> schedule(const Engine* e, bool first, bool allow_plane = true) {
     std::vector<PassDesc> s;
     const bool ite = e->beta != 0.0;
     const bool qf = e->grad_terms();
+    if (allow_plane && plane_schedule(e)) {
+        const uint32_t aux = (e->n <= ((size_t)1 << 21)) ? F_AUX_CPLX : 0u;
+        if (qf) {
+            if (first) s.push_back({AX_YZ, PRE_NONE, MID_LAP_STORE, POST_NONE, F_LAP, B_PSI, B_NONE});
+            s.push_back({AX_X, PRE_NONE, MID_QF_VSTEP1, POST_NONE, F_LAP | F_KIN | F_STORE, B_PSI, B_PSI2});
+            s.push_back({AX_YZ, PRE_NONE, MID_NONE, POST_PART12, F_KIN | F_STORE | F_QF | aux, B_PSI2, B_PSI});
+            s.push_back({AX_X, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
+            s.push_back({AX_YZ, PRE_NONE, MID_NONE, POST_VSTEP3, F_KIN | F_STORE | aux | F_FIN_STEP | F_LAP_OUT,
+                         B_PSI, B_PSI});
+        } else {
+            s.push_back({AX_YZ, PRE_VSTEP1, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI2});
+            s.push_back({AX_X, PRE_NONE, MID_NONE, POST_VSTEP2, F_KIN | F_STORE | aux, B_PSI2, B_PSI});
+            s.push_back({AX_YZ, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
+            s.push_back({AX_X, PRE_NONE, MID_NONE, POST_VSTEP3, F_KIN | F_STORE | aux | F_FIN_STEP, B_PSI, B_PSI});
+        }
+        return s;
+    }
     // corrector factor stored as complex exp(c3 V') (Vstep3 then needs no sincos) where the extra 4 bytes
     // per point stay in L2 (FP32 lattices of <= 2^21 points) and always in FP64 (ALU-bound); else the
     // real V' (FP32 on HBM-resident lattices: recomputing the phase is cheaper than moving 4 more bytes)
@@ -508,19 +543,23 @@ static PassArgs<R> base_args(const Engine* e) {
 
 template <typename R>
 static void axis_args(const Engine* e, PassArgs<R>& a, int axis) {
+    if (axis == AX_YZ) axis = AX_Z;  // the plane pass: z tables here, y tables in PlaneArgs
     a.ktab = (const C2<R>*)e->ax[axis].ktab;
     a.plan = effective_plan(e->fft_plan, e->n3[axis], e->prec == GPE_PRECISION_FP32);
     a.tw = (const C2<R>*)e->ax[axis].tw[a.plan];
     a.ld1 = (const R*)e->ax[axis].ld1;
 }
 
-static size_t pencils_of(const Engine* e, int axis) { return e->n / (size_t)e->n3[axis]; }
+static size_t pencils_of(const Engine* e, int axis) {
+    return axis == AX_YZ ? (size_t)e->n3[0] : e->n / (size_t)e->n3[axis];  // the plane pass: one CTA per x-plane
+}
 
 template <typename R>
 static PassArgs<R> desc_args(const Engine* e, const PassDesc& d) {
     PassArgs<R> a = base_args<R>(e);
     axis_args(e, a, d.axis);
-    if (!e->pass_plan.empty()) {
+    const int tax = d.axis == AX_YZ ? AX_Z : d.axis;  // axis of the tables
+    if (!e->pass_plan.empty() && d.axis != AX_YZ) {
         const uint64_t k = pass_key(d);
         for (const auto& pp : e->pass_plan)
             if (pp.first == k) {
@@ -528,7 +567,7 @@ static PassArgs<R> desc_args(const Engine* e, const PassDesc& d) {
                 a.tw = (const C2<R>*)e->ax[d.axis].tw[a.plan];
             }
     }
-    a.ltab = (const R*)e->ax[d.axis].lqf;
+    a.ltab = (const R*)e->ax[tax].lqf;
     a.in = (const C2<R>*)(d.in == B_PSI ? e->psi : e->psi2);
     a.out = (C2<R>*)(d.out == B_PSI ? e->psi : d.out == B_PSI2 ? e->psi2 : nullptr);
     a.pre = d.pre; a.mid = d.mid; a.post = d.post;
@@ -537,7 +576,7 @@ static PassArgs<R> desc_args(const Engine* e, const PassDesc& d) {
     // ops' operands where used instead of staging them, so the epilogue passes fit 7 CTAs per SM
     // (measured +6% steps/s at 128^3; at 256^3, HBM-resident, the staged prefetch is 6-12% faster).
     // The Weizsaecker sums and currents keep their slots.
-    const bool direct_ok = e->prec == GPE_PRECISION_FP32 && e->n3[d.axis] <= 128 && !(d.flags & (F_WZ | F_DIP)) &&
+    const bool direct_ok = e->prec == GPE_PRECISION_FP32 && e->n3[tax] <= 128 && !(d.flags & (F_WZ | F_DIP)) &&
                            d.mid != MID_CURRENT;
     if (direct_ok && (e->direct_mode < 0 ? e->n <= ((size_t)1 << 21) : e->direct_mode == 1)) a.flags |= F_DIRECT;
     a.npencils = (uint32_t)pencils_of(e, d.axis);
@@ -548,6 +587,17 @@ template <typename R>
 static int launch_desc(Engine* e, const PassDesc& d) {
     const PassArgs<R> a = desc_args<R>(e, d);
     e->launches++;
+    if (d.axis == AX_YZ) {
+        if constexpr (sizeof(R) == 4) {
+            PlaneArgs pa;
+            pa.a = a;
+            pa.kty = (const float2*)e->ax[AX_Y].ktab;
+            pa.lqy = (const float*)e->ax[AX_Y].lqf;
+            return cuda_rc(launch_plane(pa, e->n3[AX_Z], (unsigned)e->n3[AX_X], e->st));
+        } else {
+            return cuda_rc(cudaErrorInvalidValue);
+        }
+    }
     return cuda_rc(launch_pass<R>(a, e->n3[d.axis], d.axis, pencils_of(e, d.axis), e->st));
 }
 
@@ -625,7 +675,7 @@ static int profile_passes(Engine* e, int nsteps, float* ms, double* bytes, int* 
         ms[p] = (float)(acc[p] / nsteps);
         bytes[p] = pass_bytes(e, s[p]);
         axis[p] = s[p].axis;
-        cls[p] = op_class(s[p].pre, s[p].mid, s[p].post, s[p].flags);
+        cls[p] = s[p].axis == AX_YZ ? 8 : op_class(s[p].pre, s[p].mid, s[p].post, s[p].flags);
     }
     e->it += (unsigned)nsteps;
     if (e->beta != 0.0) {
@@ -1366,7 +1416,7 @@ static int batch_build(gpe_gb_batch* b) {
     for (size_t i = 0; i < b->eng.size(); i++)
         if (b->active[i]) { first = (int)i; break; }
     if (first < 0) { b->dirty = false; return 0; }
-    const std::vector<PassDesc> s = schedule(&b->eng[first]->e, false);
+    const std::vector<PassDesc> s = schedule(&b->eng[first]->e, false, false);  // pencil passes only
     for (const PassDesc& d : s) {
         std::vector<BatchItem<float>> items;
         size_t smem = 0;
@@ -1562,6 +1612,7 @@ int gpe_gb_change_alpha_beta(gpe_gb_engine* h, double alpha, double beta) {
     if (!h) return GPE_ERR_NO_ENGINE;
     h->e.alpha = alpha;
     h->e.beta = beta;
+    h->e.lap_valid = false;  // the pass layout (and what lap holds between steps) may change
     return gpe::upload(&h->e);
 }
 
@@ -2102,6 +2153,17 @@ int gpe_gb_control_destroy(gpe_gb_control* hc) {
     gpe::ctl_release(&hc->c);
     delete hc;
     return gpe::cuda_rc(cudaGetLastError());
+}
+
+int gpe_gb_set_plane_passes(gpe_gb_engine* h, int enable) {
+    if (!h) return GPE_ERR_NO_ENGINE;
+    Engine* e = &h->e;
+    GPE_CK(cudaStreamSynchronize(e->st));
+    e->plane_mode = enable ? -1 : 0;
+    e->lap_valid = false;  // lap holds D_z psi between pencil steps, (D_y + D_z) psi between plane steps
+    e->graph_dirty = true;
+    e->version++;
+    return 0;
 }
 
 int gpe_gb_set_fft_plan(gpe_gb_engine* h, int plan) {

@@ -767,7 +767,9 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                     // from the (user-)modified psi_n (dev/gpe_engine.cu:1040-1041, 758-760)
                     const C2<R> pm = modify_at<R>(ix, iy, iz, it, p);
 #ifdef GPE_USER_HOOKS
-                    const R rho_m = density(a.ph, pm);
+                    // an unchanged psi keeps the density already taken (recomputing it could round
+                    // differently where the compiler fuses the other product)
+                    const R rho_m = (pm.x == p.x && pm.y == p.y) ? rho : density(a.ph, pm);
 #else
                     const R rho_m = rho;
 #endif

@@ -1,0 +1,232 @@
+// yz-plane pass (FP32-mixed form): the y and z transforms of one x-plane in
+// one CTA.
+//
+// A lattice plane [iy][iz] of N x N points (N = 128: 128 KiB of FP32 complex)
+// is contiguous in memory and fits one CTA's shared memory, so the kinetic
+// factor of both axes, exp(c3 k_y^2) exp(c3 k_z^2), is applied by one 2D
+// transform pair inside the CTA instead of two pencil passes, each of which
+// reads and writes the whole field through L2.  With the pointwise ops of the
+// step fused in (Vstep1 before, the corrector or Vstep3 after) and the y+z
+// spectral Laplacian of the result (quantum friction), a real-time step takes
+// four launches (two plane passes, two x-pencil passes) instead of seven.
+//
+// Layout in shared memory: point (iy, iz) at padp(iy) * RP + padp(iz), RP =
+// padded_len<N>() (one pad slot per 16 points in both directions), so rows
+// (z pencils) and columns (y pencils) are both exchanged without bank
+// conflicts.  1024 threads: in the row phase 8 threads per row, E = 16 points
+// each, 4 rows per warp (row exchanges under warp barriers); in the column
+// phase 8 threads per column, column fastest within a warp (column exchanges
+// under CTA barriers).  Rows are loaded from and stored to global memory in
+// the z-pass pattern (8 threads x 8 B = 64 contiguous bytes per row segment).
+#pragma once
+#include "gpe_pass.cuh"
+
+namespace gpe {
+
+struct PlaneArgs {
+    PassArgs<float> a;   // field, ops, device state; a.ktab / a.ltab: z tables; a.tw: twiddles (plan 0)
+    const float2* kty;   // y kinetic factors exp(c3 k_y^2) / N_y
+    const float* lqy;    // y Laplacian weights k_y^2 / N_y
+};
+
+template <int N>
+struct PlaneGeom {
+    static constexpr int E = Plan<N, 0>::E;
+    static constexpr int T = N / E;  // threads per row / per column
+    static constexpr int NT = N * T;
+    static constexpr int RP = padded_len<N>();
+    static constexpr int TW = tw_len<N, 0>();
+    static constexpr size_t TAB_BYTES = (((size_t)(TW + 2 * N) * sizeof(float2) + 2 * N * sizeof(float)) + 15) & ~(size_t)15;
+    static constexpr size_t PLANE_BYTES = (size_t)RP * RP * sizeof(float2);
+    static constexpr size_t SMEM = TAB_BYTES + PLANE_BYTES;
+    static_assert(NT == 1024, "one plane per 1024-thread CTA");
+    static_assert(SMEM <= 225 * 1024, "plane does not fit shared memory");
+};
+
+// Ops a plane pass supports (real time only: no reductions, no pending norm factor).
+__host__ __device__ inline bool plane_supports(int pre, int mid, int post, uint32_t flags) {
+    const uint32_t allowed = F_KIN | F_STORE | F_QF | F_AUX_CPLX | F_LAP_OUT | F_FIN_STEP | F_VEXTRA | F_LAP;
+    if (flags & ~allowed) return false;
+    if (pre != PRE_NONE && pre != PRE_VSTEP1) return false;
+    if (mid != MID_NONE && mid != MID_LAP_STORE) return false;
+    if (post != POST_NONE && post != POST_PART12 && post != POST_VSTEP3) return false;
+    return true;
+}
+
+template <int N>
+__global__ void __launch_bounds__(PlaneGeom<N>::NT, 1) plane_kernel(const PlaneArgs pa) {
+    using R = float;
+    using Geo = PlaneGeom<N>;
+    constexpr int E = Geo::E, T = Geo::T, NT = Geo::NT, RP = Geo::RP;
+    const PassArgs<R>& a = pa.a;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C2<R>* stw = reinterpret_cast<C2<R>*>(smem_raw);
+    C2<R>* sky = stw + Geo::TW;
+    C2<R>* skz = sky + N;
+    R* sly = reinterpret_cast<R*>(skz + N);
+    R* slz = sly + N;
+    C2<R>* plane = reinterpret_cast<C2<R>*>(smem_raw + Geo::TAB_BYTES);
+    __shared__ double sred[NT / 32][NRED];
+    __shared__ bool last_cta;
+
+    // constant tables before the wait for the previous pass (programmatic dependent launch)
+    const int tid = threadIdx.x;
+    for (int i = tid; i < Geo::TW; i += NT) stw[i] = a.tw[i];
+    for (int i = tid; i < N; i += NT) {
+        sky[i] = pa.kty[i];
+        skz[i] = a.ktab[i];
+        sly[i] = pa.lqy[i];
+        slz[i] = a.ltab[i];
+    }
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+
+    // row phase: row iy = tid / T, points iz = tr + T q; column phase: column iz = tid % N, points iy = tc + T q
+    const int row = tid / T, tr = tid % T;
+    const int col = tid % N, tc = tid / N;
+    C2<R>* sbr = plane + padp(row) * RP;
+    C2<R>* sbc = plane + padp(col);
+    const uint32_t ix = blockIdx.x;
+    const int ly = a.ly, lz = a.lz;
+    const uint32_t rowbase = ((ix << ly) + (uint32_t)row) << lz;
+    auto at = [&](int q) -> uint32_t { return rowbase + (uint32_t)(tr + T * q); };
+    auto rcell = [&](int q) -> C2<R>& { return sbr[padp(tr + T * q)]; };
+    auto ccell = [&](int q) -> C2<R>& { return sbc[padp(tc + T * q) * RP]; };
+
+    const DynState* dyn = a.dyn;
+    const unsigned it = dyn->it;
+    C2<R> x[E];
+#pragma unroll
+    for (int q = 0; q < E; q++) x[q] = a.in[at(q)];
+#ifdef GPE_USER_HOOKS
+    if (tid < 32) gpe_hook_ctx.up[tid] = a.uparam[tid];
+    if (tid == 0) {
+        gpe_hook_ctx.nx = 1u << a.lx;
+        gpe_hook_ctx.ny = 1u << a.ly;
+        gpe_hook_ctx.nz = 1u << a.lz;
+        gpe_hook_ctx.dt = a.dt;
+        gpe_hook_ctx.t0 = a.t0;
+        gpe_hook_ctx.npart = a.npart;
+    }
+#endif
+    __syncthreads();  // tables (and hook context) staged
+
+    // ------------------------------------------------------------ PRE (row cells)
+    if (a.pre == PRE_VSTEP1) {
+#pragma unroll
+        for (int q = 0; q < E; q++) rcell(q) = x[q];
+#pragma unroll 1
+        for (int q = 0; q < E; q++) {
+            const uint32_t idx = at(q);
+            const int iz = tr + T * q;
+            C2<R> v = modify_at<R>((int)ix, row, iz, it, rcell(q));
+            const R rho = density(a.ph, v);
+            const R V = vext_at(a, idx, (int)ix, row, iz, it) + mean_field(a, rho, it);
+            a.V[idx] = V;
+            rcell(q) = cmul(v, phase(a.ph, V));
+        }
+#pragma unroll
+        for (int q = 0; q < E; q++) x[q] = rcell(q);
+        __syncwarp();
+    }
+
+    // 2D transform pair: rows forward, columns forward, x mult(k_y, k_z), columns inverse, rows inverse.
+    // `mode` 0: kinetic factors; 1: Laplacian weights (k_y^2 + k_z^2) / (N_y N_z)
+    auto pair2d = [&](int mode) {
+        fft<R, N, 0, false, 1, 32>(x, sbr, tr, stw, 0);
+        __syncwarp();  // the row's exchange reads are done before its cells are overwritten
+#pragma unroll
+        for (int q = 0; q < E; q++) rcell(q) = x[q];
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < E; q++) x[q] = ccell(q);
+        fft<R, N, 0, false, RP, NT>(x, sbc, tc, stw, 0);
+        if (mode == 0) {
+            const C2<R> kz = skz[col];
+#pragma unroll
+            for (int q = 0; q < E; q++) x[q] = cmul(cmul(x[q], sky[tc + T * q]), kz);
+        } else {
+            const R lz_ = slz[col];
+            const R inv = (R)1 / (R)N;
+#pragma unroll
+            for (int q = 0; q < E; q++) x[q] = cscale(x[q], (sly[tc + T * q] + lz_) * inv);
+        }
+        fft<R, N, 0, true, RP, NT>(x, sbc, tc, stw, 0);
+        __syncthreads();  // every column's exchange reads are done
+#pragma unroll
+        for (int q = 0; q < E; q++) ccell(q) = x[q];
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < E; q++) x[q] = rcell(q);
+        fft<R, N, 0, true, 1, 32>(x, sbr, tr, stw, 0);
+    };
+
+    if (a.flags & F_LAP) {
+        // y + z Laplacian of the input only (the first step after psi changed)
+        pair2d(1);
+#pragma unroll
+        for (int q = 0; q < E; q++) a.lap[at(q)] = x[q];
+    } else {
+        if (a.flags & F_KIN) pair2d(0);
+
+        // -------------------------------------------------------- POST (row cells)
+        if (a.post != POST_NONE) {
+            __syncwarp();
+#pragma unroll
+            for (int q = 0; q < E; q++) rcell(q) = x[q];
+#pragma unroll 1
+            for (int q = 0; q < E; q++) {
+                const uint32_t idx = at(q);
+                const int iz = tr + T * q;
+                C2<R> v = rcell(q);
+                if (a.post == POST_PART12) {
+                    R lv = a.V[idx];
+                    const C2<R> pp = cmul(v, phase(a.ph, lv));
+                    const R rho = density(a.ph, pp);
+                    lv = (lv + vext_at(a, idx, (int)ix, row, iz, it + 1)) + mean_field(a, rho, it + 1);
+                    if (a.flags & F_QF) lv += a.Vqf[idx];
+                    lv = (R)0.5 * lv;
+                    const C2<R> e = phase(a.ph, lv);
+                    if (a.flags & F_AUX_CPLX) reinterpret_cast<C2<R>*>(a.aux)[idx] = e;
+                    else reinterpret_cast<R*>(a.aux)[idx] = lv;
+                    v = cmul(modify_at<R>((int)ix, row, iz, it, a.psi[idx]), e);
+                } else {  // POST_VSTEP3
+                    const C2<R> e = (a.flags & F_AUX_CPLX) ? reinterpret_cast<const C2<R>*>(a.aux)[idx]
+                                                           : phase(a.ph, reinterpret_cast<const R*>(a.aux)[idx]);
+                    v = cmul(v, e);
+                }
+                rcell(q) = v;
+            }
+#pragma unroll
+            for (int q = 0; q < E; q++) x[q] = rcell(q);
+            __syncwarp();
+        }
+        if (a.flags & F_STORE) {
+#pragma unroll
+            for (int q = 0; q < E; q++) a.out[at(q)] = x[q];
+        }
+        if (a.flags & F_LAP_OUT) {
+            // y + z Laplacian of the result, for the next step's friction potential
+            __syncthreads();  // the plane's cells are free again
+            pair2d(1);
+#pragma unroll
+            for (int q = 0; q < E; q++) a.lap[at(q)] = x[q];
+        }
+    }
+
+    // ---------------------------------------------------- step counter (last CTA)
+    if (a.flags & F_FIN_STEP) {
+        if (tid == 0) {
+            __threadfence();
+            const unsigned prev = atomicAdd(&a.dyn->ticket, 1u);
+            last_cta = (prev == gridDim.x - 1);
+        }
+        __syncthreads();
+        if (last_cta) {
+            __threadfence();
+            finalize<R, NT, 1>(a, sred, gridDim.x, false);
+        }
+    }
+}
+
+}  // namespace gpe
