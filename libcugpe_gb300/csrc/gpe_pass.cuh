@@ -745,13 +745,19 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                 }
             } else if (a.mid == MID_QF_VSTEP1) {
                 to_cells();
+                // the Laplacian and psi of point q + 1 are loaded while point q is computed
+                C2<R> nl = op_lap(0, at(0)), np = op_copy(0, at(0));
 #pragma unroll 1
                 for (int q = 0; q < E; q++) {
                     const uint32_t idx = at(q);
+                    const C2<R> L = cadd(nl, own(q));
+                    const C2<R> p = np;
+                    if (q + 1 < E) {
+                        nl = op_lap(q + 1, at(q + 1));
+                        np = op_copy(q + 1, at(q + 1));
+                    }
                     int ix, iy, iz;
                     decode(idx, ix, iy, iz);
-                    const C2<R> L = cadd(op_lap(q, idx), own(q));
-                    const C2<R> p = op_copy(q, idx);
                     const R rho = density(a.ph, p);
                     // (qf/Gamma) Im(conj(psi) L) / (rho + eps), L = -lap psi   (dev/gpe_engine.cu:893-918)
                     R vqf = (a.ph.qf_g * (p.x * L.y + (-p.y) * L.x)) / (rho + a.ph.qf_eps);
@@ -805,34 +811,55 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
         if (a.post != POST_NONE && valid) {
             cp_async_wait_all();
             to_cells();
+            // The operands of point q + 1 are loaded while point q is computed, so that their latency
+            // (an L2 round trip where they are read in place) overlaps the transcendental work.
+            if (a.post == POST_VSTEP2 || a.post == POST_PART12) {
+                const bool qfop = (a.post == POST_PART12) && (a.flags & F_QF);
+                R nv = op_v(0, at(0)), nq = qfop ? op_vqf(0, at(0)) : (R)0;
+                C2<R> np = op_psi(0, at(0));
 #pragma unroll 1
-            for (int q = 0; q < E; q++) {
-                const uint32_t idx = at(q);
-                C2<R> v = own(q);
-                if (a.post == POST_VSTEP2 || a.post == POST_PART12) {
+                for (int q = 0; q < E; q++) {
+                    const uint32_t idx = at(q);
+                    R lv = nv;
+                    C2<R> p = np;
+                    const R vq = nq;
+                    if (q + 1 < E) {
+                        const uint32_t nidx = at(q + 1);
+                        nv = op_v(q + 1, nidx);
+                        np = op_psi(q + 1, nidx);
+                        if (qfop) nq = op_vqf(q + 1, nidx);
+                    }
                     int ix, iy, iz;
                     decode(idx, ix, iy, iz);
-                    R lv = op_v(q, idx);
-                    const C2<R> pp = cmul(v, phase(a.ph, lv));
+                    const C2<R> pp = cmul(own(q), phase(a.ph, lv));
                     const R rho = density(a.ph, pp);
                     lv = (lv + vext_at(a, idx, ix, iy, iz, it + 1)) + mean_field(a, rho, it + 1);
-                    if (a.post == POST_PART12 && (a.flags & F_QF)) lv += op_vqf(q, idx);
+                    if (qfop) lv += vq;
                     lv = (R)0.5 * lv;
                     const C2<R> e = phase(a.ph, lv);
                     if (a.flags & F_AUX_CPLX) reinterpret_cast<C2<R>*>(a.aux)[idx] = e;
                     else reinterpret_cast<R*>(a.aux)[idx] = lv;
-                    C2<R> p = op_psi(q, idx);
                     if (scale_in) p = cscale(p, s_prev);
-                    v = cmul(modify_at<R>(ix, iy, iz, it, p), e);
-                } else if (a.post == POST_PART1) {
-                    v = cmul(v, phase(a.ph, op_v(q, idx)));
-                } else if (a.post == POST_VSTEP3) {
-                    C2<R> e;
-                    if (a.flags & F_AUX_CPLX) e = direct ? reinterpret_cast<const C2<R>*>(a.aux)[idx] : slotA[q * NT + tid];
-                    else e = phase(a.ph, slotC[q * NT + tid]);
-                    v = cmul(v, e);
+                    own(q) = cmul(modify_at<R>(ix, iy, iz, it, p), e);
                 }
-                own(q) = v;
+            } else if (a.post == POST_PART1) {
+                R nv = op_v(0, at(0));
+#pragma unroll 1
+                for (int q = 0; q < E; q++) {
+                    const R lv = nv;
+                    if (q + 1 < E) nv = op_v(q + 1, at(q + 1));
+                    own(q) = cmul(own(q), phase(a.ph, lv));
+                }
+            } else if (a.post == POST_VSTEP3) {
+                if (a.flags & F_AUX_CPLX) {
+                    // the stored factor: one complex multiply per point (unrolled: all loads in flight)
+#pragma unroll
+                    for (int q = 0; q < E; q++)
+                        own(q) = cmul(own(q), direct ? reinterpret_cast<const C2<R>*>(a.aux)[at(q)] : slotA[q * NT + tid]);
+                } else {
+#pragma unroll 1
+                    for (int q = 0; q < E; q++) own(q) = cmul(own(q), phase(a.ph, slotC[q * NT + tid]));
+                }
             }
             from_cells();
         }

@@ -170,36 +170,54 @@ __global__ void __launch_bounds__(PlaneGeom<N>::NT, 1) plane_kernel(const PlaneA
         if (a.flags & F_KIN) pair2d(0);
 
         // -------------------------------------------------------- POST (row cells)
-        if (a.post != POST_NONE) {
+        if (a.post == POST_PART12) {
+            // the operands of point q + 1 are loaded while point q is computed (their L2 latency
+            // overlaps the transcendental work)
             __syncwarp();
 #pragma unroll
             for (int q = 0; q < E; q++) rcell(q) = x[q];
+            const bool qfop = (a.flags & F_QF) != 0;
+            R nv = a.V[at(0)], nq = qfop ? a.Vqf[at(0)] : (R)0;
+            C2<R> np = a.psi[at(0)];
 #pragma unroll 1
             for (int q = 0; q < E; q++) {
                 const uint32_t idx = at(q);
                 const int iz = tr + T * q;
-                C2<R> v = rcell(q);
-                if (a.post == POST_PART12) {
-                    R lv = a.V[idx];
-                    const C2<R> pp = cmul(v, phase(a.ph, lv));
-                    const R rho = density(a.ph, pp);
-                    lv = (lv + vext_at(a, idx, (int)ix, row, iz, it + 1)) + mean_field(a, rho, it + 1);
-                    if (a.flags & F_QF) lv += a.Vqf[idx];
-                    lv = (R)0.5 * lv;
-                    const C2<R> e = phase(a.ph, lv);
-                    if (a.flags & F_AUX_CPLX) reinterpret_cast<C2<R>*>(a.aux)[idx] = e;
-                    else reinterpret_cast<R*>(a.aux)[idx] = lv;
-                    v = cmul(modify_at<R>((int)ix, row, iz, it, a.psi[idx]), e);
-                } else {  // POST_VSTEP3
-                    const C2<R> e = (a.flags & F_AUX_CPLX) ? reinterpret_cast<const C2<R>*>(a.aux)[idx]
-                                                           : phase(a.ph, reinterpret_cast<const R*>(a.aux)[idx]);
-                    v = cmul(v, e);
+                R lv = nv;
+                const C2<R> p = np;
+                const R vq = nq;
+                if (q + 1 < E) {
+                    nv = a.V[at(q + 1)];
+                    np = a.psi[at(q + 1)];
+                    if (qfop) nq = a.Vqf[at(q + 1)];
                 }
-                rcell(q) = v;
+                const C2<R> pp = cmul(rcell(q), phase(a.ph, lv));
+                const R rho = density(a.ph, pp);
+                lv = (lv + vext_at(a, idx, (int)ix, row, iz, it + 1)) + mean_field(a, rho, it + 1);
+                if (qfop) lv += vq;
+                lv = (R)0.5 * lv;
+                const C2<R> e = phase(a.ph, lv);
+                if (a.flags & F_AUX_CPLX) reinterpret_cast<C2<R>*>(a.aux)[idx] = e;
+                else reinterpret_cast<R*>(a.aux)[idx] = lv;
+                rcell(q) = cmul(modify_at<R>((int)ix, row, iz, it, p), e);
             }
 #pragma unroll
             for (int q = 0; q < E; q++) x[q] = rcell(q);
             __syncwarp();
+        } else if (a.post == POST_VSTEP3) {
+            if (a.flags & F_AUX_CPLX) {
+#pragma unroll
+                for (int q = 0; q < E; q++) x[q] = cmul(x[q], reinterpret_cast<const C2<R>*>(a.aux)[at(q)]);
+            } else {
+                __syncwarp();
+#pragma unroll
+                for (int q = 0; q < E; q++) rcell(q) = x[q];
+#pragma unroll 1
+                for (int q = 0; q < E; q++) rcell(q) = cmul(rcell(q), phase(a.ph, reinterpret_cast<const R*>(a.aux)[at(q)]));
+#pragma unroll
+                for (int q = 0; q < E; q++) x[q] = rcell(q);
+                __syncwarp();
+            }
         }
         if (a.flags & F_STORE) {
 #pragma unroll
