@@ -12,7 +12,8 @@ only) and checked three ways:
 * a user header whose potential, functional and gpe_modify_psi all depend on
   the step (tests/hooks/moving_trap_kick.h) against the CPU oracle evaluating
   the same header compiled for the host;
-* the default header against the library without hooks: bit-identical in FP64.
+* the default header against the library without hooks: the same FP64 arithmetic (to the last few
+  units of rounding, which fused multiply-adds the compiler chose apart).
 """
 import os
 
@@ -182,8 +183,10 @@ DEFAULT_CASES = [
 
 @pytest.mark.parametrize("case", DEFAULT_CASES, ids=lambda c: f"{c[0]}_b{c[2]}_qf{c[4]}")
 def test_default_header_reproduces_builtin_physics(default_lib, case):
-    """FP64: bit-identical to the library without hooks, step by step and in the energy; FP32: the
-    hooks compute in FP64 before rounding, so only to FP32 accuracy."""
+    """FP64: the same arithmetic as the library without hooks; the two libraries are separately
+    compiled, and the compiler's choice of which products to fuse into multiply-adds may differ between
+    them, so agreement is to a few units of the last place (3.7e-16 relative L2 measured), not bit for
+    bit.  FP32: the hooks compute in FP64 before rounding, so only to FP32 accuracy."""
     shape, alpha, beta, dt, qf = case
     params = [0.04, 0.05, 0.06, 0.0]
     psi = configs.random_state(shape, seed=33, npart=100.0, gamma=2.0)
@@ -199,13 +202,13 @@ def test_default_header_reproduces_builtin_physics(default_lib, case):
             ma, mb = a.evolve_qf(2), b.evolve_qf(2)
             pa, pb = a.get_psi()[1], b.get_psi()[1]
             if exact:
-                assert np.array_equal(pa, pb), rel(pa, pb)
-                assert ma == mb
+                assert rel(pa, pb) <= 2e-15, rel(pa, pb)
+                assert abs(ma - mb) <= 1e-14 * max(1.0, abs(mb))
             else:
                 assert rel(pa, pb) <= 1e-5
         ea, eb = a.energy(), b.energy()
         if exact:
-            assert ea == eb
+            assert all(abs(x - y) <= 1e-14 * max(1.0, abs(y)) for x, y in zip(ea, eb))
         else:
             assert all(abs(x - y) <= 1e-5 * max(1.0, abs(y)) for x, y in zip(ea, eb))
         a.close()
