@@ -383,37 +383,17 @@ def run_batch_workload(args):
     t_tune = time.perf_counter()
     tuned = b.autotune(16)
     t_tune = time.perf_counter() - t_tune
-    done = np.zeros(len(ens), dtype=bool)
-    steps = np.zeros(len(ens), dtype=int)
-    mu_final = np.full(len(ens), np.nan)
-    sum_prev = np.full(len(ens), np.nan)
-    mean_prev = np.full(len(ens), np.nan)
-    last_change = np.full(len(ens), np.nan)
     torch.cuda.synchronize()
     l0 = b.kernel_launches()
     t0 = time.perf_counter()
-    total = 0
-    while not done.all() and total < max_steps:
-        b.evolve(check)
-        total += check
-        _, msum = b.chemical_potentials()
-        for i in np.nonzero(~done)[0]:
-            steps[i] += check
-            # the mu of one step from an FP32 field jitters at ~1e-7; the change of the
-            # interval mean (mean of `check` steps) between intervals does not
-            if np.isfinite(sum_prev[i]):
-                mean = (msum[i] - sum_prev[i]) / check
-                if np.isfinite(mean_prev[i]):
-                    last_change[i] = abs(mean - mean_prev[i]) / check / dx2[i]
-                    if last_change[i] < tol:
-                        done[i] = True
-                        mu_final[i] = mean / dx2[i]
-                        b.set_active(int(i), False)
-                mean_prev[i] = mean
-            sum_prev[i] = msum[i]
+    # convergence test on the device: the interval mean of mu (lattice units) changes by < tol dx^2 per
+    # step between consecutive intervals of `check` steps; a converged condensate is retired at once
+    steps, mu_lat = b.solve(max_steps, check, tol * dx2)
     t_batch = time.perf_counter() - t0
     launches = b.kernel_launches() - l0
-    # the unconverged: their last interval change, and what FP64 needs on the same problem
+    done = steps >= 0
+    mu_final = np.where(done, mu_lat / dx2, np.nan)
+    # the unconverged, and what FP64 needs on the same problem
     stragglers = []
     for i in np.nonzero(~done)[0][: args.batch_diag]:
         c = ens[i]
@@ -423,10 +403,9 @@ def run_batch_workload(args):
         st64, mu64 = solve_until(e.evolve_qf, e.chemical_potential, c["dx"] ** 2, tol, check, max_steps)
         e.close()
         stragglers.append({"n": c["shape"][0], "gN": c["params"][3] * c["dx"] * 4 * np.pi,
-                           "omega_ratio": c["params"][2] / c["params"][0], "fp32_steps": int(steps[i]),
-                           "fp32_last_change_per_step": float(last_change[i]),
+                           "omega_ratio": c["params"][2] / c["params"][0], "fp32_steps": int(max_steps),
                            "fp64_steps_to_converge": int(st64),
-                           "fp32_vs_fp64_mu": float(abs(mean_prev[i] / dx2[i] - mu64) / abs(mu64)) if mu64 else None})
+                           "fp32_vs_fp64_mu": float(abs(mu_lat[i] / dx2[i] - mu64) / abs(mu64)) if mu64 else None})
     # serial FP64 loop: one condensate at a time, same criterion; a stated subset per size
     per_size = {}
     subset = args.batch_serial_subset

@@ -175,8 +175,9 @@ int gpe_gb_norm_noalloc(const void* psi, int precision, long long n, double gamm
  * beta; FP32-mixed only.  Every fused pass of a step is one launch over all active
  * condensates, whatever their sizes, and runs of steps replay from one
  * captured CUDA graph.  Per-condensate parameters, psi and observables go
- * through the condensate's engine handle (gpe_gb_batch_engine); quantum
- * friction is not supported in a batch. */
+ * through the condensate's engine handle (gpe_gb_batch_engine).  All active
+ * condensates must run the same step (all imaginary or all real time, all with
+ * or all without quantum friction); the Weizsaecker term is not supported. */
 typedef struct gpe_gb_batch gpe_gb_batch;
 int gpe_gb_batch_create(gpe_gb_batch** out, int count, const int* sides, int interactions, int precision,
                         double alpha, double beta, const double* dt, const double* npart);
@@ -186,6 +187,16 @@ gpe_gb_engine* gpe_gb_batch_engine(gpe_gb_batch* b, int i);
 int gpe_gb_batch_set_active(gpe_gb_batch* b, int i, int active);
 /* nt steps of every active condensate (gpe_evolve_qf semantics per condensate). */
 int gpe_gb_batch_evolve(gpe_gb_batch* b, int nt);
+/* Imaginary-time solve of every active condensate (no reference counterpart):
+ * each condensate steps until the mean of mu over an interval of `check` steps
+ * differs from the previous interval's mean by less than tol[i] per step
+ * (lattice units), at most max_steps steps.  The test runs on the device at the
+ * end of every step and retires a converged condensate at once (its passes are
+ * skipped from the next step on); the host reads the retirement flags once per
+ * replayed graph.  Out: steps[i] = steps to convergence (-1: not converged),
+ * mu[i] = the converged interval mean (the last step's mu if not converged).
+ * The pending normalisation is applied on return, as after gpe_gb_batch_evolve. */
+int gpe_gb_batch_solve(gpe_gb_batch* b, int max_steps, int check, const double* tol, int* steps, double* mu);
 /* Per condensate: mu of the last ITE step and the running sum of mu. */
 int gpe_gb_batch_chemical_potentials(gpe_gb_batch* b, double* mu, double* mu_sum);
 long long gpe_gb_batch_kernel_launches(const gpe_gb_batch* b);

@@ -51,7 +51,7 @@ C_ABI_SYMBOLS = [
     "gpe_gb_snapshots_close", "gpe_gb_dftc_write_info", "gpe_gb_dftc_read_info", "gpe_gb_set_weizsacker",
     "gpe_gb_evolve_dipolar", "gpe_gb_energy_dipolar", "gpe_gb_autotune", "gpe_gb_batch_autotune",
     "gpe_gb_set_fft_plan", "gpe_gb_get_fft_plan", "gpe_gb_batch_set_fft_plan", "gpe_gb_fp64_fma_rate",
-    "gpe_gb_user_hooks", "gpe_gb_set_plane_passes",
+    "gpe_gb_user_hooks", "gpe_gb_set_plane_passes", "gpe_gb_batch_solve",
 ]
 
 
@@ -113,6 +113,7 @@ def _lib(path: str | None = None):
             "gpe_gb_fp64_fma_rate": (i, [dp]),
             "gpe_gb_user_hooks": (i, [ip, ip]),
             "gpe_gb_set_plane_passes": (i, [vp, i]),
+            "gpe_gb_batch_solve": (i, [vp, i, i, dp, ip, dp]),
             "gpe_gb_set_vortex": (i, [vp, d, d, i]),
             "gpe_gb_get_phase": (i, [vp, dp]),
             "gpe_gb_set_phase": (i, [vp, dp]),
@@ -425,6 +426,20 @@ class Batch:
     def set_fft_plan(self, plan):
         """Radix plan of every condensate's pencil FFTs (0 default, 1 alternative)."""
         _check(self._L.gpe_gb_batch_set_fft_plan(self._h, int(plan)), "batch_set_fft_plan", self._L)
+
+    def solve(self, max_steps, check, tol):
+        """Imaginary-time solve with the convergence test on the device: each active condensate stops
+        once the mean of mu over `check` steps changes by less than tol (per step, lattice units; a
+        scalar or one value per condensate) between intervals.  Returns (steps, mu): steps to
+        convergence (-1 if not converged within max_steps) and the converged interval mean of mu."""
+        n = len(self.engines)
+        t = np.ascontiguousarray(np.broadcast_to(np.asarray(tol, dtype=np.float64), (n,)))
+        steps = np.zeros(n, dtype=np.int32)
+        mu = np.zeros(n)
+        _check(self._L.gpe_gb_batch_solve(self._h, int(max_steps), int(check), _dp(t),
+                                          steps.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _dp(mu)),
+               "batch_solve", self._L)
+        return steps, mu
 
     def chemical_potentials(self):
         """Per condensate: (mu of the last ITE step, running sum of mu)."""

@@ -60,6 +60,24 @@ __global__ void k_set_state(DynState* d, unsigned it, double s_prev) {
     d->s_prev = s_prev;
     d->s2 = 1.0;
     d->ticket = 0;
+    d->retired = 0;
+    d->conv_check = 0;
+}
+
+// Arms (check > 0) or clears (check = 0) the device-side convergence test of a batched solve.
+__global__ void k_conv_setup(DynState* d, unsigned check, double tol) {
+    d->conv_check = check;
+    d->conv_tol = tol;
+    d->conv_start = d->mu_sum;
+    d->conv_n = 0;
+    d->conv_have = 0;
+    d->retired = 0;
+}
+
+// retired[i] = the retirement flag of condensate i
+__global__ void k_gather_retired(DynState* const* dyn, int n, unsigned* retired) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) retired[i] = dyn[i]->retired;
 }
 
 __global__ void k_reset_scale(DynState* d) { d->s_prev = 1.0; }
@@ -1392,6 +1410,7 @@ struct gpe_gb_batch {
     int order = 0;    // item order in a launch: 0 as created, 1 most CTAs first (autotuner)
     int chunk = 16;   // steps per replayed graph (autotuner)
     int plan = 0;     // radix plan of every condensate's pencil FFTs (autotuner)
+    bool warm = false;  // the current launches ran once outside capture (kernel attributes set)
 };
 
 namespace gpe {
@@ -1402,6 +1421,7 @@ static void batch_free_items(gpe_gb_batch* b) {
     if (b->gexec) cudaGraphExecDestroy(b->gexec);
     b->gexec = nullptr;
     b->gsteps = 0;
+    b->warm = false;
 }
 
 template <int AX>
@@ -1478,21 +1498,48 @@ static int batch_steps(gpe_gb_batch* b, int k) {
     return 0;
 }
 
-static int batch_evolve(gpe_gb_batch* b, int nt) {
+// Steps every active condensate `nt` times (no post-processing; see batch_evolve).  Every active
+// condensate must run the same pass sequence: all imaginary or all real time, all with or all without
+// quantum friction (no Weizsaecker term).  With friction, the first step after a condensate's psi
+// changed also forms its z-Laplacian: that step runs for each condensate on its own.
+static int batch_run(gpe_gb_batch* b, int nt) {
     if (nt <= 0) return 0;
     bool stale = b->dirty;
+    int first = -1;
+    bool need_first_step = false;
     for (size_t i = 0; i < b->eng.size(); i++) {
         Engine* e = &b->eng[i]->e;
         if (!b->active[i]) continue;
-        if (e->grad_terms() || e->prec != GPE_PRECISION_FP32) return GPE_ERR_ARGUMENT;
+        if (e->wz != 0.0 || e->prec != GPE_PRECISION_FP32) return GPE_ERR_ARGUMENT;
+        if (first < 0) first = (int)i;
+        const Engine* f = &b->eng[first]->e;
+        if ((e->beta != 0.0) != (f->beta != 0.0) || e->grad_terms() != f->grad_terms()) return GPE_ERR_ARGUMENT;
+        if (e->grad_terms() && !e->lap_valid) need_first_step = true;
         if (e->version != b->built_version[i]) stale = true;
+    }
+    if (first < 0) return 0;
+    int done = 0;
+    if (need_first_step) {
+        for (size_t i = 0; i < b->eng.size(); i++) {
+            if (!b->active[i]) continue;
+            Engine* e = &b->eng[i]->e;
+            GPE_CK(cudaStreamSynchronize(b->st));
+            GPE_RC(run_steps(e, schedule(e, e->grad_terms() && !e->lap_valid, false), 1));
+            e->lap_valid = e->grad_terms();
+            GPE_CK(cudaStreamSynchronize(e->st));
+        }
+        done = 1;
+        if (nt == 1) return 0;
     }
     if (stale) GPE_RC(batch_build(b));
     if (b->passes.empty()) return 0;
-    int done = 0;
-    // one direct step first (configures the kernels outside capture), then graph replays
-    GPE_RC(batch_steps(b, 1));
-    done = 1;
+    // the first step after the launches were built runs directly (configures the kernels outside
+    // capture), then graph replays
+    if (!b->warm) {
+        GPE_RC(batch_steps(b, 1));
+        done += 1;
+        b->warm = true;
+    }
     const int chunk = b->chunk;
     if (nt - done >= chunk && b->gsteps != chunk) {
         cudaGraph_t g = nullptr;
@@ -1515,16 +1562,91 @@ static int batch_evolve(gpe_gb_batch* b, int nt) {
         done += b->gsteps;
     }
     GPE_RC(batch_steps(b, nt - done));
-    GPE_CK(cudaStreamSynchronize(b->st));
+    return cuda_rc(cudaStreamSynchronize(b->st));
+}
+
+static int batch_evolve(gpe_gb_batch* b, int nt) {
+    if (nt <= 0) return 0;
+    GPE_RC(batch_run(b, nt));
     for (size_t i = 0; i < b->eng.size(); i++) {
         if (!b->active[i]) continue;
         Engine* e = &b->eng[i]->e;
-        if (e->beta != 0.0) GPE_RC(finish_ite<float>(e));
+        if (e->beta != 0.0) {
+            GPE_RC(finish_ite<float>(e));
+            e->lap_valid = false;  // psi was rescaled
+        }
         e->it += (unsigned)nt;
     }
     for (size_t i = 0; i < b->eng.size(); i++)
         if (b->active[i]) GPE_CK(cudaStreamSynchronize(b->eng[i]->e.st));
     return 0;
+}
+
+// Imaginary-time solve of every active condensate with the convergence test on the device: each
+// condensate's last pass of a step compares the mean of mu over the last `check` steps with the mean
+// over the interval before (DynState conv_*) and retires the condensate once they differ by less than
+// tol[i] per step; every pass then skips it.  The host reads the retirement flags once per replayed
+// graph (one copy of n flags) and drops the retired condensates from the launches.
+static int batch_solve(gpe_gb_batch* b, int max_steps, int check, const double* tol, int* steps, double* mu) {
+    const size_t n = b->eng.size();
+    if (max_steps < 1 || check < 1 || !tol || !steps || !mu) return GPE_ERR_ARGUMENT;
+    const std::vector<char> initial = b->active;
+    std::vector<unsigned> it0(n, 0);
+    for (size_t i = 0; i < n; i++) {
+        if (!initial[i]) continue;
+        Engine* e = &b->eng[i]->e;
+        if (e->beta == 0.0 || !(tol[i] >= 0.0)) return GPE_ERR_ARGUMENT;
+        GPE_CK(cudaStreamSynchronize(e->st));
+        k_conv_setup<<<1, 1, 0, b->st>>>(e->dyn, (unsigned)check, tol[i]);
+        it0[i] = e->it;
+    }
+    GPE_CK(cudaGetLastError());
+    DynState** ddyn = nullptr;
+    unsigned* dflag = nullptr;
+    std::vector<DynState*> hdyn(n);
+    std::vector<unsigned> flag(n, 0);
+    for (size_t i = 0; i < n; i++) hdyn[i] = b->eng[i]->e.dyn;
+    int rc = cuda_rc(cudaMalloc(&ddyn, sizeof(DynState*) * n));
+    if (!rc) rc = cuda_rc(cudaMalloc(&dflag, sizeof(unsigned) * n));
+    if (!rc) rc = cuda_rc(cudaMemcpyAsync(ddyn, hdyn.data(), sizeof(DynState*) * n, cudaMemcpyHostToDevice, b->st));
+    int done = 0;
+    while (!rc && done < max_steps) {
+        const int k = (max_steps - done < b->chunk) ? max_steps - done : b->chunk;
+        rc = batch_run(b, k);
+        if (rc) break;
+        done += k;
+        k_gather_retired<<<(unsigned)((n + 127) / 128), 128, 0, b->st>>>(ddyn, (int)n, dflag);
+        rc = cuda_rc(cudaMemcpyAsync(flag.data(), dflag, sizeof(unsigned) * n, cudaMemcpyDeviceToHost, b->st));
+        if (!rc) rc = cuda_rc(cudaStreamSynchronize(b->st));
+        bool any = false;
+        for (size_t i = 0; i < n; i++) {
+            if (b->active[i] && flag[i]) { b->active[i] = 0; b->dirty = true; }
+            any = any || b->active[i];
+        }
+        if (!any) break;
+    }
+    cudaFree(ddyn);
+    cudaFree(dflag);
+    // results; the pending normalisation is applied and the test cleared, as after evolve
+    for (size_t i = 0; i < n && !rc; i++) {
+        if (!initial[i]) continue;
+        Engine* e = &b->eng[i]->e;
+        DynState h;
+        rc = cuda_rc(cudaMemcpyAsync(&h, e->dyn, sizeof h, cudaMemcpyDeviceToHost, b->st));
+        if (!rc) rc = cuda_rc(cudaStreamSynchronize(b->st));
+        if (rc) break;
+        const bool conv = h.retired != 0;
+        steps[i] = conv ? (int)(h.conv_step - it0[i]) : -1;
+        mu[i] = conv ? h.conv_mu : h.mu;
+        e->it = it0[i] + (unsigned)(conv ? steps[i] : done);
+        k_conv_setup<<<1, 1, 0, e->st>>>(e->dyn, 0u, 0.0);
+        rc = finish_ite<float>(e);
+        e->lap_valid = false;
+        if (!rc) rc = cuda_rc(cudaStreamSynchronize(e->st));
+    }
+    b->active = initial;
+    b->dirty = true;
+    return rc;
 }
 
 }  // namespace gpe
@@ -2039,6 +2161,11 @@ int gpe_gb_batch_set_active(gpe_gb_batch* b, int i, int active) {
 int gpe_gb_batch_evolve(gpe_gb_batch* b, int nt) {
     if (!b) return GPE_ERR_NO_ENGINE;
     return gpe::batch_evolve(b, nt);
+}
+
+int gpe_gb_batch_solve(gpe_gb_batch* b, int max_steps, int check, const double* tol, int* steps, double* mu) {
+    if (!b) return GPE_ERR_NO_ENGINE;
+    return gpe::batch_solve(b, max_steps, check, tol, steps, mu);
 }
 
 int gpe_gb_batch_chemical_potentials(gpe_gb_batch* b, double* mu, double* mu_sum) {

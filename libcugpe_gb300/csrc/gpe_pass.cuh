@@ -85,10 +85,22 @@ struct DynState {
     double dmu;        // change of mu over the last step
     double mu_sum;     // running sum of mu over ITE steps (interval means for convergence tests)
     double red[16];    // results of generic reductions
+    // device-side convergence test of a batched imaginary-time solve (gpe_gb_batch_solve): every
+    // conv_check steps the mean of mu over the interval is compared with the previous interval's
+    double conv_tol;   // retire when the interval means differ by less than conv_tol per step
+    double conv_start; // mu_sum at the start of the current interval
+    double conv_prev;  // mean of mu over the previous interval
+    double conv_mu;    // interval mean at retirement
     unsigned int it;   // step counter since set_psi / set_time
     unsigned int ticket;
     unsigned int err;
     unsigned int pad;
+    unsigned int conv_check;  // steps per interval (0: no test)
+    unsigned int conv_n;      // steps into the current interval
+    unsigned int conv_have;   // a previous interval mean exists
+    unsigned int retired;     // converged: every pass of a batch skips this condensate
+    unsigned int conv_step;   // step counter `it` after the step that converged
+    unsigned int pad2[3];
 };
 
 constexpr int NRED = 3;
@@ -270,6 +282,18 @@ __device__ void finalize(const PassArgs<R>& a, double (*sred)[NRED], uint32_t nb
                 d->dmu = mu - d->mu;
                 d->mu = mu;
                 d->mu_sum += mu;
+                if (d->conv_check && ++d->conv_n == d->conv_check) {
+                    const double mean = (d->mu_sum - d->conv_start) / (double)d->conv_check;
+                    if (d->conv_have && fabs(mean - d->conv_prev) < d->conv_tol * (double)d->conv_check) {
+                        d->retired = 1;
+                        d->conv_step = d->it + 1;
+                        d->conv_mu = mean;
+                    }
+                    d->conv_prev = mean;
+                    d->conv_have = 1;
+                    d->conv_start = d->mu_sum;
+                    d->conv_n = 0;
+                }
             }
             d->it = d->it + 1;
         }
@@ -440,6 +464,8 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     }
     asm volatile("griddepcontrol.wait;" ::: "memory");
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    // a condensate that a batched solve has retired (converged) is left as it is
+    if (a.dyn->retired) return;
 
     int pl, t, bar;
     C2<R>* sb;
