@@ -246,6 +246,7 @@ struct Engine {
     int vortex_q = 1;
     bool vortex_set = false, phase_set = false;
     int vslices = 0, vsteps = 1;
+    int vring = 0;  // vextra holds a two-slot ring of slices (set by the control problem)
 
     bool use_graph = true;
     int direct_mode = -1;   // operands read where used: -1 by lattice size, 0 staged, 1 direct (autotuner)
@@ -548,6 +549,7 @@ static PassArgs<R> base_args(const Engine* e) {
     a.vextra = (const R*)e->vextra;
     a.vsteps = e->vsteps * e->sub;
     a.vslices = e->vslices;
+    a.vring = e->vring;
     a.dyn = e->dyn;
     a.partials = e->partials;
     a.lx = e->l3[0]; a.ly = e->l3[1]; a.lz = e->l3[2];
@@ -1054,7 +1056,8 @@ struct Control {
     int nbasis = 0, nslices = 0, sps = 1, ck = 100;
     double* basis = nullptr;     // [nbasis][n]
     double* controls = nullptr;  // [nslices][nbasis]
-    double* fields = nullptr;    // [nslices][n]
+    double* fields = nullptr;    // [2][n]: slice s of the control potential in slot s & 1
+    int slot_slice[2] = {-1, -1};  // which slice each slot holds
     double2* target = nullptr;
     double2* ckpt = nullptr;     // checkpoints
     int nckpt = 0;
@@ -1089,7 +1092,7 @@ __device__ __forceinline__ int ctl_slice(const CtlArgs& a, unsigned it) {
 }
 __device__ __forceinline__ double ctl_vext(const CtlArgs& a, size_t i, unsigned it) {
     const int ix = (int)(i >> (a.ly + a.lz)), iy = (int)((i >> a.lz) & ((1u << a.ly) - 1)), iz = (int)(i & ((1u << a.lz) - 1));
-    return (a.vx[ix] + a.vy[iy]) + a.vz[iz] + a.fields[(size_t)ctl_slice(a, it) * a.n + i];
+    return (a.vx[ix] + a.vy[iy]) + a.vz[iz] + a.fields[(size_t)(ctl_slice(a, it) & 1) * a.n + i];
 }
 __device__ __forceinline__ double2 ctl_phase(double c3y, double V) {
     double s, c;
@@ -1101,13 +1104,13 @@ __device__ __forceinline__ double ctl_vbar(double c3y, double2 w, double2 wb) {
     return -c3y * (w.y * wb.x - w.x * wb.y);
 }
 
-__global__ void k_ctl_fields(const double* c, const double* basis, double* fields, int nslices, int nbasis, size_t n) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        for (int s = 0; s < nslices; s++) {
-            double v = 0.0;
-            for (int k = 0; k < nbasis; k++) v += c[s * nbasis + k] * basis[(size_t)k * n + i];
-            fields[(size_t)s * n + i] = v;
-        }
+// field = sum_k c[slice][k] G_k (one slice of the control potential)
+__global__ void k_ctl_field(const double* c, const double* basis, double* field, int slice, int nbasis, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        double v = 0.0;
+        for (int k = 0; k < nbasis; k++) v += c[slice * nbasis + k] * basis[(size_t)k * n + i];
+        field[i] = v;
+    }
 }
 
 // partial sums of conj(t) psi, then the last block publishes the overlap
@@ -1177,8 +1180,10 @@ __global__ void __launch_bounds__(kCtlThreads) k_ctl_bw2(CtlArgs a, const double
                                                         const double* Wbar, const double2* Cbar, double2* AB, double* Vbar,
                                                         double2* bar, const double* basis, int nbasis, double* part) {
     __shared__ double sp[kCtlMaxBasis][kCtlThreads / 32];
+    // per-basis partial projections in registers: every index below is a compile-time constant
     double acc[kCtlMaxBasis];
-    for (int k = 0; k < nbasis; k++) acc[k] = 0.0;
+#pragma unroll
+    for (int k = 0; k < kCtlMaxBasis; k++) acc[k] = 0.0;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < a.n; i += (size_t)gridDim.x * blockDim.x) {
         const double2 F = ctl_phase(a.c3y, W[i]);
         const double2 cb = Cbar[i];
@@ -1190,13 +1195,18 @@ __global__ void __launch_bounds__(kCtlThreads) k_ctl_bw2(CtlArgs a, const double
         const double2 Pb = make_double2(a.g * wb * P.x, a.g * wb * P.y);
         AB[i] = cmulc(Pb, E);
         Vbar[i] = 0.5 * wb + ctl_vbar(a.c3y, P, Pb);
-        for (int k = 0; k < nbasis; k++) acc[k] += basis[(size_t)k * a.n + i] * (0.5 * wb);
+#pragma unroll
+        for (int k = 0; k < kCtlMaxBasis; k++)
+            if (k < nbasis) acc[k] += basis[(size_t)k * a.n + i] * (0.5 * wb);
     }
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int k = 0; k < nbasis; k++) {
-        double v = acc[k];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0) sp[k][w] = v;
+#pragma unroll
+    for (int k = 0; k < kCtlMaxBasis; k++) {
+        if (k < nbasis) {
+            double v = acc[k];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) sp[k][w] = v;
+        }
     }
     __syncthreads();
     if ((int)threadIdx.x < nbasis) {
@@ -1212,8 +1222,10 @@ __global__ void __launch_bounds__(kCtlThreads) k_ctl_bw3(CtlArgs a, const double
                                                         const double2* Abar, const double* Vbar, double2* bar,
                                                         const double* basis, int nbasis, double* part) {
     __shared__ double sp[kCtlMaxBasis][kCtlThreads / 32];
+    // per-basis partial projections in registers: every index below is a compile-time constant
     double acc[kCtlMaxBasis];
-    for (int k = 0; k < nbasis; k++) acc[k] = 0.0;
+#pragma unroll
+    for (int k = 0; k < kCtlMaxBasis; k++) acc[k] = 0.0;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < a.n; i += (size_t)gridDim.x * blockDim.x) {
         const double2 E = ctl_phase(a.c3y, Vn[i]);
         const double2 p = psi[i];
@@ -1225,13 +1237,18 @@ __global__ void __launch_bounds__(kCtlThreads) k_ctl_bw3(CtlArgs a, const double
         b.x += e.x + 2.0 * a.g * vb * p.x;
         b.y += e.y + 2.0 * a.g * vb * p.y;
         bar[i] = b;
-        for (int k = 0; k < nbasis; k++) acc[k] += basis[(size_t)k * a.n + i] * vb;
+#pragma unroll
+        for (int k = 0; k < kCtlMaxBasis; k++)
+            if (k < nbasis) acc[k] += basis[(size_t)k * a.n + i] * vb;
     }
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int k = 0; k < nbasis; k++) {
-        double v = acc[k];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0) sp[k][w] = v;
+#pragma unroll
+    for (int k = 0; k < kCtlMaxBasis; k++) {
+        if (k < nbasis) {
+            double v = acc[k];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) sp[k][w] = v;
+        }
     }
     __syncthreads();
     if ((int)threadIdx.x < nbasis) {
@@ -1290,15 +1307,49 @@ static int ctl_kinetic(Control* c, double2* buf, int conj) {
     return 0;
 }
 
+// The control potential of step `it` and of its corrector (`it` + 1) are slices slice_of(it) and
+// slice_of(it + 1): ensures both are in the ring (they are consecutive, so they occupy both slots).
+static int ctl_slice_of(const Control* c, unsigned it) {
+    const int s = (int)(it / (unsigned)c->sps);
+    return s >= c->nslices ? c->nslices - 1 : s;
+}
+static int ctl_fill(Control* c, unsigned it) {
+    Engine* e = c->e;
+    for (int s : {ctl_slice_of(c, it), ctl_slice_of(c, it + 1)}) {
+        if (c->slot_slice[s & 1] == s) continue;
+        k_ctl_field<<<1024, 256, 0, e->st>>>(c->controls, c->basis, c->fields + (size_t)(s & 1) * e->n, s, c->nbasis,
+                                            e->n);
+        c->slot_slice[s & 1] = s;
+        e->launches++;
+    }
+    return cuda_rc(cudaGetLastError());
+}
+
+// `m` forward steps from the engine's current step, in pieces that stay within one slice (whose
+// corrector may reach into the next), refilling the ring before each piece.
+static int ctl_steps(Control* c, int m) {
+    Engine* e = c->e;
+    while (m > 0) {
+        const unsigned it = e->it;
+        const int s = ctl_slice_of(c, it);
+        int piece = (s == c->nslices - 1) ? m : (int)((unsigned)(s + 1) * (unsigned)c->sps - it);
+        if (piece > m) piece = m;
+        GPE_RC(ctl_fill(c, it));
+        GPE_RC(evolve(e, piece, nullptr));
+        m -= piece;
+    }
+    return 0;
+}
+
 static int ctl_forward(Control* c, const double* controls_host, const double* psi0_host, double* loss, double2* o_out) {
     Engine* e = c->e;
     const size_t n = e->n;
     GPE_CK(cudaMemcpyAsync(c->controls, controls_host, sizeof(double) * c->nslices * c->nbasis, cudaMemcpyHostToDevice, e->st));
-    k_ctl_fields<<<1024, 256, 0, e->st>>>(c->controls, c->basis, c->fields, c->nslices, c->nbasis, n);
-    GPE_CK(cudaGetLastError());
+    c->slot_slice[0] = c->slot_slice[1] = -1;  // new controls: both slots are stale
     e->vextra = c->fields;
     e->vslices = c->nslices;
     e->vsteps = c->sps;
+    e->vring = 1;
     e->graph_dirty = true;
     e->version++;
     GPE_CK(cudaMemcpyAsync(e->psi, psi0_host, sizeof(double2) * n, cudaMemcpyHostToDevice, e->st));
@@ -1308,7 +1359,7 @@ static int ctl_forward(Control* c, const double* controls_host, const double* ps
     const int nseg = c->nckpt - 1;
     for (int j = 0; j < nseg; j++) {
         GPE_CK(cudaMemcpyAsync(c->ckpt + (size_t)j * n, e->psi, sizeof(double2) * n, cudaMemcpyDeviceToDevice, e->st));
-        GPE_RC(evolve(e, c->ck, nullptr));
+        GPE_RC(ctl_steps(c, c->ck));
     }
     GPE_CK(cudaMemcpyAsync(c->ckpt + (size_t)nseg * n, e->psi, sizeof(double2) * n, cudaMemcpyDeviceToDevice, e->st));
     k_ctl_overlap<<<kCtlBlocks, kCtlThreads, 0, e->st>>>(c->target, (const double2*)e->psi, n, c->ovl);
@@ -1336,11 +1387,12 @@ static int ctl_backward(Control* c, double2 o, double* grad_host) {
         GPE_RC(set_state(e, e->it, 1.0));
         for (int i = 0; i < c->ck; i++) {
             GPE_CK(cudaMemcpyAsync(c->seg + (size_t)i * n, e->psi, sizeof(double2) * n, cudaMemcpyDeviceToDevice, e->st));
-            GPE_RC(evolve(e, 1, nullptr));
+            GPE_RC(ctl_steps(c, 1));
         }
         for (int i = c->ck - 1; i >= 0; i--) {
             const unsigned it = (unsigned)(j * c->ck + i);
             const double2* psi = c->seg + (size_t)i * n;
+            GPE_RC(ctl_fill(c, it));
             k_ctl_fw1<<<1024, 256, 0, e->st>>>(a, it, psi, c->Vn, c->bufA);
             GPE_RC(ctl_kinetic(c, c->bufA, 0));
             k_ctl_fw2<<<1024, 256, 0, e->st>>>(a, it, psi, c->Vn, c->bufA, c->W, c->bufC);
@@ -1370,6 +1422,7 @@ static void ctl_release(Control* c) {
     if (c->e && c->e->vextra == c->fields) {
         c->e->vextra = nullptr;
         c->e->vslices = 0;
+        c->e->vring = 0;
         c->e->graph_dirty = true;
         c->e->version++;
     }
@@ -2008,6 +2061,7 @@ int gpe_gb_set_potential_slices(gpe_gb_engine* h, const double* fields, int nsli
     if (!h) return GPE_ERR_NO_ENGINE;
     Engine* e = &h->e;
     cudaStreamSynchronize(e->st);
+    if (e->vring) return GPE_ERR_ARGUMENT;  // the engine's time-sliced potential belongs to a control problem
     cudaFree(e->vextra);
     e->vextra = nullptr;
     e->vslices = 0;
@@ -2221,7 +2275,7 @@ int gpe_gb_control_create(gpe_gb_control** out, gpe_gb_engine* h, int nbasis, co
     };
     alloc((void**)&c->basis, sizeof(double) * nbasis * n);
     alloc((void**)&c->controls, sizeof(double) * nslices * nbasis);
-    alloc((void**)&c->fields, sizeof(double) * nslices * n);
+    alloc((void**)&c->fields, sizeof(double) * 2 * n);
     alloc((void**)&c->target, sizeof(double2) * n);
     alloc((void**)&c->ckpt, sizeof(double2) * n * c->nckpt);
     alloc((void**)&c->seg, sizeof(double2) * n * c->ck);

@@ -120,8 +120,9 @@ struct PassArgs {
     const R* ld1;        // k_a / N_a of this axis (first derivative)
     const R* kgx; const R* kgy; const R* kgz;  // k grids of the three axes (dipolar kernel)
     const R* vx; const R* vy; const R* vz;   // trap tables
-    const R* vextra;     // [slices][n] additive potential (F_VEXTRA)
+    const R* vextra;     // [slices][n] additive potential (F_VEXTRA); [2][n] ring when vring
     int vsteps, vslices;
+    int vring;           // vextra holds two slices: slice s in slot s & 1 (the control problem)
     const C2<R>* ktab;   // kinetic factors of this axis, incl. 1/N_a
     const R* ltab;       // Laplacian / kinetic-energy weights of this axis
     const C2<R>* tw;     // stage twiddles of this axis's radix plan
@@ -151,6 +152,7 @@ template <typename R> __device__ __forceinline__ R vext_at(const PassArgs<R>& a,
     if (a.flags & F_VEXTRA) {
         int s = (int)(it / (unsigned)a.vsteps);
         if (s >= a.vslices) s = a.vslices - 1;
+        if (a.vring) s &= 1;
         v += a.vextra[((size_t)s << (a.lx + a.ly + a.lz)) | idx];
     }
     return v;
