@@ -1307,15 +1307,16 @@ static int ctl_kinetic(Control* c, double2* buf, int conj) {
     return 0;
 }
 
-// The control potential of step `it` and of its corrector (`it` + 1) are slices slice_of(it) and
-// slice_of(it + 1): ensures both are in the ring (they are consecutive, so they occupy both slots).
+// Steps it .. it + m - 1 evaluate the control potential at it .. it + m (the corrector of the last
+// step at it + m), slices slice_of(it) .. slice_of(it + m); callers keep that range within two
+// consecutive slices, which then occupy both slots of the ring.
 static int ctl_slice_of(const Control* c, unsigned it) {
     const int s = (int)(it / (unsigned)c->sps);
     return s >= c->nslices ? c->nslices - 1 : s;
 }
-static int ctl_fill(Control* c, unsigned it) {
+static int ctl_fill(Control* c, unsigned it, unsigned m = 1) {
     Engine* e = c->e;
-    for (int s : {ctl_slice_of(c, it), ctl_slice_of(c, it + 1)}) {
+    for (int s : {ctl_slice_of(c, it), ctl_slice_of(c, it + m)}) {
         if (c->slot_slice[s & 1] == s) continue;
         k_ctl_field<<<1024, 256, 0, e->st>>>(c->controls, c->basis, c->fields + (size_t)(s & 1) * e->n, s, c->nbasis,
                                             e->n);
@@ -1334,7 +1335,7 @@ static int ctl_steps(Control* c, int m) {
         const int s = ctl_slice_of(c, it);
         int piece = (s == c->nslices - 1) ? m : (int)((unsigned)(s + 1) * (unsigned)c->sps - it);
         if (piece > m) piece = m;
-        GPE_RC(ctl_fill(c, it));
+        GPE_RC(ctl_fill(c, it, (unsigned)piece));
         GPE_RC(evolve(e, piece, nullptr));
         m -= piece;
     }
