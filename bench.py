@@ -769,7 +769,7 @@ def main():
                 "points_steps_per_s": value * n,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic, "traffic_how": traffic_how,
-                             "kernel": "pass_kernel (fused pencil pass; 7 launches per GPE step)",
+                             "kernel": "plane_kernel + pass_kernel (two yz-plane passes and two x-pencil passes per GPE step)",
                              "basis": f"B_alg {B_ALG[('fp32', True)]} B/pt/step x {n} pts / {1e6 * gpe_step_s:.2f} us "
                                       f"per GPE step (= ms_per_step / {args.block}, CUDA events on the engine "
                                       f"stream); peak {kind}; traffic = ncu DRAM bytes per GPE step",

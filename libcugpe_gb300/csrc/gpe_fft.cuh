@@ -49,12 +49,28 @@ __host__ __device__ __forceinline__ constexpr double cos16(int m) {
 }
 __host__ __device__ __forceinline__ constexpr double sin16(int m) { return cos16(m - 4); }
 
-// x * exp(-+ 2 pi i k / M) with compile-time k, M (M | 16); '-' forward, '+' inverse.
+// cos and sin of 2 pi m / 32 (the odd multiples of 2 pi / 32 that radix-32 butterflies add)
+__host__ __device__ __forceinline__ constexpr double cos32(int m) {
+    constexpr double c[9] = {1.0, 0.98078528040323044913, 0.92387953251128675613, 0.83146961230254523708,
+                             0.70710678118654752440, 0.55557023301960222474, 0.38268343236508977173,
+                             0.19509032201612826785, 0.0};
+    m &= 31;
+    return m <= 8 ? c[m] : m <= 16 ? -c[16 - m] : m <= 24 ? -c[m - 16] : c[32 - m];
+}
+__host__ __device__ __forceinline__ constexpr double sin32(int m) { return cos32(m - 8); }
+
+// x * exp(-+ 2 pi i k / M) with compile-time k, M (M | 32); '-' forward, '+' inverse.
 // Multiplications by +-1 and +-i cost nothing; the four 45-degree angles cost
-// two multiplies.
+// two multiplies.  Angles that are multiples of 2 pi / 16 take exactly the
+// same operations whatever M is.
 template <typename R, bool INV>
 __device__ __forceinline__ C2<R> rot(C2<R> x, int M, int k) {
-    const int m = (k * (16 / M)) & 15;
+    const int m32 = (k * (32 / M)) & 31;
+    if (m32 & 1) {
+        const R cr = (R)cos32(m32), sr = (R)(INV ? sin32(m32) : -sin32(m32));
+        return mk<R>(x.x * cr - x.y * sr, x.x * sr + x.y * cr);
+    }
+    const int m = m32 >> 1;
     const double c = cos16(m);
     const double s = INV ? sin16(m) : -sin16(m);
     if (m == 0) return x;
@@ -77,7 +93,7 @@ template <int BITS> __host__ __device__ __forceinline__ constexpr int bitrev(int
 }
 __host__ __device__ __forceinline__ constexpr int ilog2c(int x) { return x <= 1 ? 0 : 1 + ilog2c(x / 2); }
 
-// In-register DFT of RAD points (RAD in {2,4,8,16}), natural order in and
+// In-register DFT of RAD points (RAD in {2,4,8,16,32}), natural order in and
 // out.  Radix-2 decimation in frequency with compile-time twiddles; the final
 // bit reversal is a compile-time register renaming.
 template <typename R, int RAD, bool INV>
@@ -120,7 +136,8 @@ template <> struct Plan<32, 1> { static constexpr int E = 16, L = 2, R0 = 16, R1
 template <> struct Plan<64, 1> { static constexpr int E = 16, L = 2, R0 = 16, R1 = 4, R2 = 1; };
 template <> struct Plan<128, 1> { static constexpr int E = 8, L = 3, R0 = 8, R1 = 8, R2 = 2; };
 template <> struct Plan<256, 1> { static constexpr int E = 8, L = 3, R0 = 8, R1 = 8, R2 = 4; };
-template <> struct Plan<512, 1> { static constexpr int E = 16, L = 3, R0 = 8, R1 = 8, R2 = 8; };
+// 512 points at 32 per thread: radix 32 then 16, one exchange per transform instead of two
+template <> struct Plan<512, 1> { static constexpr int E = 32, L = 2, R0 = 32, R1 = 16, R2 = 1; };
 __host__ __device__ constexpr bool has_plan1(int n) { return n >= 32 && n <= 512; }
 
 template <int N, int P, int S> __host__ __device__ constexpr int plan_rad() {

@@ -88,7 +88,7 @@ cudaError_t launch_ax(const PassArgs<R>& a, size_t pencils, cudaStream_t st, uns
             // FP32 x pencils of 512 points: the persistent pass overlaps loads and transforms (measured
             // at 512^3 with 16 points per thread: 923 -> 809 us per pass; on y pencils, at either point
             // count, and at 256 points it was slower)
-            if constexpr (sizeof(R) == 4 && N >= 512 && AX == AX_X) {
+            if constexpr (sizeof(R) == 4 && N >= 512 && AX == AX_X && Plan<N, P>::E <= 16) {
                 if ((a.flags & ~(F_VEXTRA | F_DIRECT)) == (F_KIN | F_STORE) && a.pre == PRE_NONE &&
                     a.mid == MID_NONE && a.post == POST_NONE)
                     return launch_one<R, N, AX, NT, C_KINP, P>(a, pencils, st);
