@@ -498,6 +498,11 @@ def run_cool512_workload(args):
     e.set_quantum_friction_coeff(w.qf)
     e.set_psi(0.0, w.psi0)
     e0 = sum(e.energy()[1:]) / dx ** 2
+    # launch configuration chosen by the autotuner (radix plan per fused pass, graph length), outside
+    # the timed region; it restores psi, time and step counter
+    t_tune = time.perf_counter()
+    tuned = e.autotune(8)
+    t_tune = time.perf_counter() - t_tune
     stream = torch.cuda.ExternalStream(e.stream_handle())
     with Clocks(0) as clk:
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -538,6 +543,7 @@ def run_cool512_workload(args):
                                               "fp64_256_initial": f0 / w.npart, "fp64_256_final": f1 / w.npart,
                                               "final_rel_diff": abs(e1 - f1) / abs(f1)},
             "fp64_256_seconds": t64, "clocks": clk.summary(),
+            "autotune": dict(tuned, seconds=t_tune, note="before the timed run, state restored"),
             "config": {"workload": "cooling run: 512^3, dx=0.1, UFG, quantum friction 0.2, omega=1, 8 vortex lines "
                                    "(charge +1, seeded in the disk r<4), dt=2e-3, %d steps, npart=5e4"
                                    % w.steps, "lattice": list(w.shape)}}
