@@ -563,9 +563,11 @@ static PassArgs<R> base_args(const Engine* e) {
 
 template <typename R>
 static void axis_args(const Engine* e, PassArgs<R>& a, int axis) {
-    if (axis == AX_YZ) axis = AX_Z;  // the plane pass: z tables here, y tables in PlaneArgs
+    const bool plane = axis == AX_YZ;
+    if (plane) axis = AX_Z;  // the plane pass: z tables here, y tables in PlaneArgs
     a.ktab = (const C2<R>*)e->ax[axis].ktab;
-    a.plan = effective_plan(e->fft_plan, e->n3[axis], e->prec == GPE_PRECISION_FP32);
+    // the plane pass has one radix plan (plan 0) whatever the pencil passes run
+    a.plan = plane ? 0 : effective_plan(e->fft_plan, e->n3[axis], e->prec == GPE_PRECISION_FP32);
     a.tw = (const C2<R>*)e->ax[axis].tw[a.plan];
     a.ld1 = (const R*)e->ax[axis].ld1;
 }

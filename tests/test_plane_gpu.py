@@ -126,3 +126,29 @@ def test_switch_between_layouts_mid_run(cuda_device, gpe_lib):
     assert rel(a.get_psi()[1], b.get_psi()[1]) <= 5e-5
     a.close()
     b.close()
+
+
+def test_plane_layout_with_alternative_radix_plan_and_autotuner(cuda_device, gpe_lib):
+    """The x-pencil passes may run the alternative radix plan (by hand or chosen by the autotuner) while
+    the plane passes keep theirs; the autotuner restores the state."""
+    case = "ufg_rte_qf"
+    shape, inter, qf, params, npart = CASES[case]
+    psi = start(case, seed=15)
+    e = engine(case, psi)
+    e.set_fft_plan(1)
+    e.evolve_qf(4)
+    o = oracle.Oracle(shape, inter, 1.0, 0.0, 0.05, npart, threads=8)
+    o.set_user_params(params)
+    o.set_quantum_friction_coeff(qf)
+    o.set_psi(0.0, psi)
+    o.evolve_qf(4)
+    assert rel(e.get_psi()[1], o.get_psi()[1]) <= 4 * 2e-5
+    e.set_fft_plan(0)
+    before = e.get_psi()
+    choice = e.autotune(8)
+    assert choice["ms_per_step"] > 0 and choice["fft_plan"] in (0, 1, 2)
+    after = e.get_psi()
+    assert after[0] == before[0] and np.array_equal(after[1], before[1])
+    kinds = [p["kind"] for p in e.profile_passes(1)]
+    assert kinds.count("plane") == 2, kinds
+    e.close()
