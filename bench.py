@@ -622,6 +622,8 @@ def run_lattice_workload(args):
     shape = tuple(int(x) for x in args.lattice.split(","))
     prec = g.FP32 if args.precision == "fp32" else g.FP64
     e = g.Engine(shape, 0, 1.0, 0.0, 0.02, 1e5, precision=prec)
+    if args.plan:
+        e.set_fft_plan(args.plan)
     e.set_user_params([0.002, 0.002, 0.003, 0.0])
     e.set_quantum_friction_coeff(0.1)
     e.set_psi(0.0, configs.random_state(shape, seed=3, npart=1e5, gamma=2.0))
@@ -633,7 +635,7 @@ def run_lattice_workload(args):
     secs = time.perf_counter() - t0
     e.close()
     return {"metric": "seeded run for profilers (wall clock, not a benchmark)", "lattice": list(shape),
-            "precision": args.precision, "steps": args.steps, "seconds": secs}
+            "precision": args.precision, "plan": args.plan, "steps": args.steps, "seconds": secs}
 
 
 def main():
@@ -654,6 +656,7 @@ def main():
     ap.add_argument("--lattice", default="512,512,128")
     ap.add_argument("--warm", type=int, default=3)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--plan", type=int, default=0, help="radix plan of the lattice workload's pencils (0 or 1)")
     ap.add_argument("--cool-steps", type=int, default=5000)
     ap.add_argument("--control-steps", type=int, default=2000)
     ap.add_argument("--control-ckpt", type=int, default=100)
