@@ -40,17 +40,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 def _reference_root() -> str:
-    """The reference checkout: $GPE_REFERENCE_ROOT, else the `reference_path` recorded in the
-    repository's benchmark spec; empty when neither names one."""
-    root = os.environ.get("GPE_REFERENCE_ROOT", "")
-    if root:
-        return root
-    try:
-        import json
-        with open(os.path.join(os.path.dirname(HERE), "BASELINE.json")) as fh:
-            return str(json.load(fh).get("reference_path", "") or "")
-    except (OSError, ValueError):
-        return ""
+    """The reference checkout this recipe reads: $GPE_REFERENCE_ROOT, else the path of the read-only
+    checkout on the build machine.  On machines without it (the GPU machine), `build` compiles the edited
+    copies already written to oracle/_ref/src."""
+    return os.environ.get("GPE_REFERENCE_ROOT", "") or "/root/reference"
 
 
 REF_ROOT = _reference_root()
