@@ -152,3 +152,33 @@ def test_plane_layout_with_alternative_radix_plan_and_autotuner(cuda_device, gpe
     kinds = [p["kind"] for p in e.profile_passes(1)]
     assert kinds.count("plane") == 2, kinds
     e.close()
+
+
+@pytest.mark.parametrize("what", ["vortex", "slices"])
+def test_plane_layout_with_enforced_phase_and_time_sliced_potential(cuda_device, gpe_lib, what):
+    """The plane passes under the phase-enforcing evolution (gpe_evolve_vortex, method 1) and with a
+    time-sliced additive potential, against the FP64 oracle."""
+    case = "bec_rte_qf"
+    shape, inter, qf, params, npart = CASES[case]
+    psi = start(case, seed=16)
+    e = engine(case, psi)
+    o = oracle.Oracle(shape, inter, 1.0, 0.0, 0.05, npart, threads=8)
+    o.set_user_params(params)
+    o.set_quantum_friction_coeff(qf)
+    o.set_psi(0.0, psi)
+    if what == "vortex":
+        e.set_vortex(0.5, -0.5, 1)
+        o.set_vortex(0.5, -0.5, 1)
+        e.evolve_vortex(3, 1)
+        o.evolve_vortex(3, 1)
+    else:
+        rng = np.random.default_rng(17)
+        fields = 0.002 * rng.standard_normal((3,) + shape)
+        e.set_potential_slices(fields, 2)
+        o.set_vextra(fields, 2)
+        e.evolve_qf(6)
+        o.evolve_qf(6)
+    kinds = [p["kind"] for p in e.profile_passes(1)]
+    assert kinds.count("plane") == 2, kinds
+    assert rel(e.get_psi()[1], o.get_psi()[1]) <= 6 * 2e-5
+    e.close()
