@@ -178,7 +178,7 @@ def test_plane_layout_with_enforced_phase_and_time_sliced_potential(cuda_device,
         o.set_vextra(fields, 2)
         e.evolve_qf(6)
         o.evolve_qf(6)
-    kinds = [p["kind"] for p in e.profile_passes(1)]
-    assert kinds.count("plane") == 2, kinds
     assert rel(e.get_psi()[1], o.get_psi()[1]) <= 6 * 2e-5
+    kinds = [p["kind"] for p in e.profile_passes(1)]  # (steps further: after the comparison)
+    assert kinds.count("plane") == 2, kinds
     e.close()
