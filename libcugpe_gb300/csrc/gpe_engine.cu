@@ -461,16 +461,19 @@ static std::vector<PassDesc> schedule(const Engine* e, bool first, bool allow_pl
     const bool qf = e->grad_terms();
     if (allow_plane && plane_schedule(e)) {
         const uint32_t aux = (e->n <= ((size_t)1 << 21)) ? F_AUX_CPLX : 0u;
+        // with a complex aux buffer, Vstep1 leaves exp(c3 V) there for the corrector (which then
+        // overwrites it with its own factor)
+        const uint32_t phs = aux ? F_PH_STORE : 0u, phl = aux ? F_PH_LOAD : 0u;
         if (qf) {
             if (first) s.push_back({AX_YZ, PRE_NONE, MID_LAP_STORE, POST_NONE, F_LAP, B_PSI, B_NONE});
-            s.push_back({AX_X, PRE_NONE, MID_QF_VSTEP1, POST_NONE, F_LAP | F_KIN | F_STORE, B_PSI, B_PSI2});
-            s.push_back({AX_YZ, PRE_NONE, MID_NONE, POST_PART12, F_KIN | F_STORE | F_QF | aux, B_PSI2, B_PSI});
+            s.push_back({AX_X, PRE_NONE, MID_QF_VSTEP1, POST_NONE, F_LAP | F_KIN | F_STORE | phs, B_PSI, B_PSI2});
+            s.push_back({AX_YZ, PRE_NONE, MID_NONE, POST_PART12, F_KIN | F_STORE | F_QF | aux | phl, B_PSI2, B_PSI});
             s.push_back({AX_X, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
             s.push_back({AX_YZ, PRE_NONE, MID_NONE, POST_VSTEP3, F_KIN | F_STORE | aux | F_FIN_STEP | F_LAP_OUT,
                          B_PSI, B_PSI});
         } else {
-            s.push_back({AX_YZ, PRE_VSTEP1, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI2});
-            s.push_back({AX_X, PRE_NONE, MID_NONE, POST_VSTEP2, F_KIN | F_STORE | aux, B_PSI2, B_PSI});
+            s.push_back({AX_YZ, PRE_VSTEP1, MID_NONE, POST_NONE, F_KIN | F_STORE | phs, B_PSI, B_PSI2});
+            s.push_back({AX_X, PRE_NONE, MID_NONE, POST_VSTEP2, F_KIN | F_STORE | aux | phl, B_PSI2, B_PSI});
             s.push_back({AX_YZ, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
             s.push_back({AX_X, PRE_NONE, MID_NONE, POST_VSTEP3, F_KIN | F_STORE | aux | F_FIN_STEP, B_PSI, B_PSI});
         }
@@ -480,17 +483,21 @@ static std::vector<PassDesc> schedule(const Engine* e, bool first, bool allow_pl
     // per point stay in L2 (FP32 lattices of <= 2^21 points) and always in FP64 (ALU-bound); else the
     // real V' (FP32 on HBM-resident lattices: recomputing the phase is cheaper than moving 4 more bytes)
     const uint32_t aux = (e->prec == GPE_PRECISION_FP64 || e->n <= ((size_t)1 << 21)) ? F_AUX_CPLX : 0u;
+    // with a complex aux buffer, Vstep1 leaves exp(c3 V) there for the corrector (part1), which then
+    // overwrites it with the corrector's own factor
+    const uint32_t phs = aux ? F_PH_STORE : 0u, phl = aux ? F_PH_LOAD : 0u;
     const uint32_t sin_ = ite ? F_SCALE_IN : 0u;
     if (!qf) {
-        s.push_back({AX_Z, PRE_VSTEP1, MID_NONE, POST_NONE, F_KIN | F_STORE | sin_, B_PSI, B_PSI2});
+        s.push_back({AX_Z, PRE_VSTEP1, MID_NONE, POST_NONE, F_KIN | F_STORE | sin_ | phs, B_PSI, B_PSI2});
         s.push_back({AX_Y, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI2, B_PSI2});
         if (!ite) {
-            s.push_back({AX_X, PRE_NONE, MID_NONE, POST_VSTEP2, F_KIN | F_STORE | aux, B_PSI2, B_PSI});
+            s.push_back({AX_X, PRE_NONE, MID_NONE, POST_VSTEP2, F_KIN | F_STORE | aux | phl, B_PSI2, B_PSI});
             s.push_back({AX_Z, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
             s.push_back({AX_Y, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
             s.push_back({AX_X, PRE_NONE, MID_NONE, POST_VSTEP3, F_KIN | F_STORE | aux | F_FIN_STEP, B_PSI, B_PSI});
         } else {
-            s.push_back({AX_X, PRE_NONE, MID_NONE, POST_PART1, F_KIN | F_STORE | F_REDUCE | F_FIN_S2, B_PSI2, B_PSI2});
+            s.push_back({AX_X, PRE_NONE, MID_NONE, POST_PART1, F_KIN | F_STORE | F_REDUCE | F_FIN_S2 | phl, B_PSI2,
+                         B_PSI2});
             s.push_back({AX_Z, PRE_PART2, MID_NONE, POST_NONE, F_KIN | F_STORE | F_SCALE_IN | F_SCALE_PSI2 | aux,
                          B_PSI, B_PSI});
             s.push_back({AX_Y, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
@@ -502,16 +509,17 @@ static std::vector<PassDesc> schedule(const Engine* e, bool first, bool allow_pl
         // step (F_LAP_OUT); the first step after psi changed computes it.
         if (first) s.push_back({AX_Z, PRE_NONE, MID_LAP_STORE, POST_NONE, F_LAP | sin_, B_PSI, B_NONE});
         s.push_back({AX_Y, PRE_NONE, MID_LAP_ACC, POST_NONE, F_LAP | sin_, B_PSI, B_NONE});
-        s.push_back({AX_X, PRE_NONE, MID_QF_VSTEP1, POST_NONE, F_LAP | F_KIN | F_STORE | sin_, B_PSI, B_PSI2});
+        s.push_back({AX_X, PRE_NONE, MID_QF_VSTEP1, POST_NONE, F_LAP | F_KIN | F_STORE | sin_ | phs, B_PSI, B_PSI2});
         s.push_back({AX_Y, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI2, B_PSI2});
         if (!ite) {
-            s.push_back({AX_Z, PRE_NONE, MID_NONE, POST_PART12, F_KIN | F_STORE | F_QF | aux, B_PSI2, B_PSI});
+            s.push_back({AX_Z, PRE_NONE, MID_NONE, POST_PART12, F_KIN | F_STORE | F_QF | aux | phl, B_PSI2, B_PSI});
             s.push_back({AX_X, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
             s.push_back({AX_Y, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
             s.push_back({AX_Z, PRE_NONE, MID_NONE, POST_VSTEP3, F_KIN | F_STORE | aux | F_FIN_STEP | F_LAP_OUT, B_PSI,
                          B_PSI});
         } else {
-            s.push_back({AX_Z, PRE_NONE, MID_NONE, POST_PART1, F_KIN | F_STORE | F_REDUCE | F_FIN_S2, B_PSI2, B_PSI2});
+            s.push_back({AX_Z, PRE_NONE, MID_NONE, POST_PART1, F_KIN | F_STORE | F_REDUCE | F_FIN_S2 | phl, B_PSI2,
+                         B_PSI2});
             s.push_back({AX_X, PRE_PART2, MID_NONE, POST_NONE,
                          F_KIN | F_STORE | F_SCALE_IN | F_SCALE_PSI2 | F_QF | aux, B_PSI, B_PSI});
             s.push_back({AX_Y, PRE_NONE, MID_NONE, POST_NONE, F_KIN | F_STORE, B_PSI, B_PSI});
@@ -659,6 +667,8 @@ static double pass_bytes(const Engine* e, const PassDesc& d) {
     if (d.post == POST_PART1) b += r;
     if (d.post == POST_VSTEP3) b += A;
     if (d.flags & F_LAP_OUT) b += S;
+    if (d.flags & F_PH_STORE) b += S;
+    if (d.flags & F_PH_LOAD) b += S;
     return b * (double)e->n;
 }
 

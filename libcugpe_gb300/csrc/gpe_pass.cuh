@@ -65,6 +65,8 @@ enum : uint32_t {  // flags
     F_DIP = 1u << 15,       // dipolar convolution pass (mid = DIP_* mode)
     F_SCALE_OPD = 1u << 16, // dipolar step: the staged psi is scaled by the pending norm factor
     F_DIRECT = 1u << 17,    // psi, V, V_qf, lap and the psi copy are read where used, not staged
+    F_PH_STORE = 1u << 18,  // Vstep1 also stores its phase factor exp(c3 V) in the (complex) aux buffer
+    F_PH_LOAD = 1u << 19,   // the corrector takes exp(c3 V) from aux instead of recomputing it
 };
 enum : int {  // dipolar pass modes (in `mid` with F_DIP)
     DIP_DENS_FWD = 1,  // x = (Gamma |psi|^2, 0), forward FFT_a -> out      (dev/gpe_engine.cu:618-626)
@@ -647,7 +649,9 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                     const R rho = density(a.ph, v);
                     const R V = vext_at(a, idx, ix, iy, iz, it) + mean_field(a, rho, it);
                     a.V[idx] = V;
-                    v = cmul(v, phase(a.ph, V));
+                    const C2<R> ph = phase(a.ph, V);
+                    if (a.flags & F_PH_STORE) reinterpret_cast<C2<R>*>(a.aux)[idx] = ph;
+                    v = cmul(v, ph);
                 } else if (K == C_EPI && a.pre == PRE_PART2) {
                     C2<R> p2 = a.psi2[idx];
                     if (a.flags & F_SCALE_PSI2) p2 = cscale(p2, s2);
@@ -809,7 +813,9 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
 #endif
                     const R V = (vext_at(a, idx, ix, iy, iz, it) + mean_field(a, rho_m, it)) + vqf;
                     a.V[idx] = V;
-                    own(q) = cmul(pm, phase(a.ph, V));
+                    const C2<R> ph = phase(a.ph, V);
+                    if (a.flags & F_PH_STORE) reinterpret_cast<C2<R>*>(a.aux)[idx] = ph;
+                    own(q) = cmul(pm, ph);
                 }
                 from_cells();
             } else if (a.mid == MID_CURRENT) {
@@ -843,23 +849,28 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
             // (an L2 round trip where they are read in place) overlaps the transcendental work.
             if (a.post == POST_VSTEP2 || a.post == POST_PART12) {
                 const bool qfop = (a.post == POST_PART12) && (a.flags & F_QF);
+                // the predictor's phase factor exp(c3 V), stored by Vstep1 (the same bits as recomputing it)
+                const bool phl = (a.flags & F_PH_LOAD) != 0;
+                const C2<R>* auxc = reinterpret_cast<const C2<R>*>(a.aux);
                 R nv = op_v(0, at(0)), nq = qfop ? op_vqf(0, at(0)) : (R)0;
-                C2<R> np = op_psi(0, at(0));
+                C2<R> np = op_psi(0, at(0)), nph = phl ? auxc[at(0)] : mk<R>((R)0, (R)0);
 #pragma unroll 1
                 for (int q = 0; q < E; q++) {
                     const uint32_t idx = at(q);
                     R lv = nv;
                     C2<R> p = np;
+                    const C2<R> ph = nph;
                     const R vq = nq;
                     if (q + 1 < E) {
                         const uint32_t nidx = at(q + 1);
                         nv = op_v(q + 1, nidx);
                         np = op_psi(q + 1, nidx);
                         if (qfop) nq = op_vqf(q + 1, nidx);
+                        if (phl) nph = auxc[nidx];
                     }
                     int ix, iy, iz;
                     decode(idx, ix, iy, iz);
-                    const C2<R> pp = cmul(own(q), phase(a.ph, lv));
+                    const C2<R> pp = cmul(own(q), phl ? ph : phase(a.ph, lv));
                     const R rho = density(a.ph, pp);
                     lv = (lv + vext_at(a, idx, ix, iy, iz, it + 1)) + mean_field(a, rho, it + 1);
                     if (qfop) lv += vq;
@@ -871,12 +882,18 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                     own(q) = cmul(modify_at<R>(ix, iy, iz, it, p), e);
                 }
             } else if (a.post == POST_PART1) {
-                R nv = op_v(0, at(0));
+                if (a.flags & F_PH_LOAD) {  // exp(c3 V) as Vstep1 stored it
+                    const C2<R>* auxc = reinterpret_cast<const C2<R>*>(a.aux);
+#pragma unroll
+                    for (int q = 0; q < E; q++) own(q) = cmul(own(q), auxc[at(q)]);
+                } else {
+                    R nv = op_v(0, at(0));
 #pragma unroll 1
-                for (int q = 0; q < E; q++) {
-                    const R lv = nv;
-                    if (q + 1 < E) nv = op_v(q + 1, at(q + 1));
-                    own(q) = cmul(own(q), phase(a.ph, lv));
+                    for (int q = 0; q < E; q++) {
+                        const R lv = nv;
+                        if (q + 1 < E) nv = op_v(q + 1, at(q + 1));
+                        own(q) = cmul(own(q), phase(a.ph, lv));
+                    }
                 }
             } else if (a.post == POST_VSTEP3) {
                 if (a.flags & F_AUX_CPLX) {

@@ -45,7 +45,8 @@ struct PlaneGeom {
 
 // Ops a plane pass supports (real time only: no reductions, no pending norm factor).
 __host__ __device__ inline bool plane_supports(int pre, int mid, int post, uint32_t flags) {
-    const uint32_t allowed = F_KIN | F_STORE | F_QF | F_AUX_CPLX | F_LAP_OUT | F_FIN_STEP | F_VEXTRA | F_LAP;
+    const uint32_t allowed = F_KIN | F_STORE | F_QF | F_AUX_CPLX | F_LAP_OUT | F_FIN_STEP | F_VEXTRA | F_LAP |
+                             F_PH_STORE | F_PH_LOAD;
     if (flags & ~allowed) return false;
     if (pre != PRE_NONE && pre != PRE_VSTEP1) return false;
     if (mid != MID_NONE && mid != MID_LAP_STORE) return false;
@@ -123,7 +124,9 @@ __global__ void __launch_bounds__(PlaneGeom<N>::NT, 1) plane_kernel(const PlaneA
             const R rho = density(a.ph, v);
             const R V = vext_at(a, idx, (int)ix, row, iz, it) + mean_field(a, rho, it);
             a.V[idx] = V;
-            rcell(q) = cmul(v, phase(a.ph, V));
+            const C2<R> ph = phase(a.ph, V);
+            if (a.flags & F_PH_STORE) reinterpret_cast<C2<R>*>(a.aux)[idx] = ph;
+            rcell(q) = cmul(v, ph);
         }
 #pragma unroll
         for (int q = 0; q < E; q++) x[q] = rcell(q);
@@ -177,21 +180,25 @@ __global__ void __launch_bounds__(PlaneGeom<N>::NT, 1) plane_kernel(const PlaneA
 #pragma unroll
             for (int q = 0; q < E; q++) rcell(q) = x[q];
             const bool qfop = (a.flags & F_QF) != 0;
+            const bool phl = (a.flags & F_PH_LOAD) != 0;  // exp(c3 V) as Vstep1 stored it
+            const C2<R>* auxc = reinterpret_cast<const C2<R>*>(a.aux);
             R nv = a.V[at(0)], nq = qfop ? a.Vqf[at(0)] : (R)0;
-            C2<R> np = a.psi[at(0)];
+            C2<R> np = a.psi[at(0)], nph = phl ? auxc[at(0)] : mk<R>((R)0, (R)0);
 #pragma unroll 1
             for (int q = 0; q < E; q++) {
                 const uint32_t idx = at(q);
                 const int iz = tr + T * q;
                 R lv = nv;
                 const C2<R> p = np;
+                const C2<R> ph = nph;
                 const R vq = nq;
                 if (q + 1 < E) {
                     nv = a.V[at(q + 1)];
                     np = a.psi[at(q + 1)];
                     if (qfop) nq = a.Vqf[at(q + 1)];
+                    if (phl) nph = auxc[at(q + 1)];
                 }
-                const C2<R> pp = cmul(rcell(q), phase(a.ph, lv));
+                const C2<R> pp = cmul(rcell(q), phl ? ph : phase(a.ph, lv));
                 const R rho = density(a.ph, pp);
                 lv = (lv + vext_at(a, idx, (int)ix, row, iz, it + 1)) + mean_field(a, rho, it + 1);
                 if (qfop) lv += vq;
