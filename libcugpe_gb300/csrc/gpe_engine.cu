@@ -461,9 +461,7 @@ static std::vector<PassDesc> schedule(const Engine* e, bool first, bool allow_pl
     const bool qf = e->grad_terms();
     if (allow_plane && plane_schedule(e)) {
         const uint32_t aux = (e->n <= ((size_t)1 << 21)) ? F_AUX_CPLX : 0u;
-        // with a complex aux buffer, Vstep1 leaves exp(c3 V) there for the corrector (which then
-        // overwrites it with its own factor)
-        const uint32_t phs = aux ? F_PH_STORE : 0u, phl = aux ? F_PH_LOAD : 0u;
+        const uint32_t phs = 0u, phl = 0u;  // FP32: recomputing exp(c3 V) costs no more than storing it
         if (qf) {
             if (first) s.push_back({AX_YZ, PRE_NONE, MID_LAP_STORE, POST_NONE, F_LAP, B_PSI, B_NONE});
             s.push_back({AX_X, PRE_NONE, MID_QF_VSTEP1, POST_NONE, F_LAP | F_KIN | F_STORE | phs, B_PSI, B_PSI2});
@@ -483,9 +481,11 @@ static std::vector<PassDesc> schedule(const Engine* e, bool first, bool allow_pl
     // per point stay in L2 (FP32 lattices of <= 2^21 points) and always in FP64 (ALU-bound); else the
     // real V' (FP32 on HBM-resident lattices: recomputing the phase is cheaper than moving 4 more bytes)
     const uint32_t aux = (e->prec == GPE_PRECISION_FP64 || e->n <= ((size_t)1 << 21)) ? F_AUX_CPLX : 0u;
-    // with a complex aux buffer, Vstep1 leaves exp(c3 V) there for the corrector (part1), which then
-    // overwrites it with the corrector's own factor
-    const uint32_t phs = aux ? F_PH_STORE : 0u, phl = aux ? F_PH_LOAD : 0u;
+    // FP64 (ALU-bound): Vstep1 leaves exp(c3 V) in the complex aux buffer for the corrector (part1),
+    // which then overwrites it with the corrector's own factor; FP32 recomputes it (measured at 128^3:
+    // the extra store and load cost as much as the sincos saved)
+    const uint32_t phs = (e->prec == GPE_PRECISION_FP64) ? F_PH_STORE : 0u;
+    const uint32_t phl = (e->prec == GPE_PRECISION_FP64) ? F_PH_LOAD : 0u;
     const uint32_t sin_ = ite ? F_SCALE_IN : 0u;
     if (!qf) {
         s.push_back({AX_Z, PRE_VSTEP1, MID_NONE, POST_NONE, F_KIN | F_STORE | sin_ | phs, B_PSI, B_PSI2});
