@@ -10,13 +10,16 @@
 // spectral Laplacian of the result (quantum friction), a real-time step takes
 // four launches (two plane passes, two x-pencil passes) instead of seven.
 //
-// Layout in shared memory: point (iy, iz) at padp(iy) * RP + padp(iz), RP =
-// padded_len<N>() (one pad slot per 16 points in both directions), so rows
-// (z pencils) and columns (y pencils) are both exchanged without bank
-// conflicts.  1024 threads: in the row phase 8 threads per row, E = 16 points
-// each, 4 rows per warp (row exchanges under warp barriers); in the column
-// phase 8 threads per column, column fastest within a warp (column exchanges
-// under CTA barriers).  Rows are loaded from and stored to global memory in
+// Layout in shared memory: point (iy, iz) at padp(iy) * RP + padp(iz), with
+// one pad slot per 16 points along each row and a row pitch RP = 146 slots
+// (RP = 2 mod 16).  1024 threads; every 128-point row and every 128-point
+// column is transformed by 8 threads of one warp (16 points each), so all
+// transform exchanges run under warp barriers and the CTA meets only where
+// rows hand over to columns and back.  Row phase: a half-warp holds two rows
+// four apart (their slots differ by 4 RP = 8 mod 16); column phase: a
+// half-warp holds two adjacent columns, each thread of a column on its own row
+// (rows differ by RP = 2 mod 16): both phases address 16 distinct 8-byte bank
+// pairs per half-warp.  Rows are loaded from and stored to global memory in
 // the z-pass pattern (8 threads x 8 B = 64 contiguous bytes per row segment).
 #pragma once
 #include "gpe_pass.cuh"
@@ -34,10 +37,13 @@ struct PlaneGeom {
     static constexpr int E = Plan<N, 0>::E;
     static constexpr int T = N / E;  // threads per row / per column
     static constexpr int NT = N * T;
-    static constexpr int RP = padded_len<N>();
+    static constexpr int ROWS = padded_len<N>();            // padded row index range
+    static constexpr int RP = ((padded_len<N>() + 13) / 16) * 16 + 2;  // row pitch, = 2 mod 16
     static constexpr int TW = tw_len<N, 0>();
     static constexpr size_t TAB_BYTES = (((size_t)(TW + 2 * N) * sizeof(float2) + 2 * N * sizeof(float)) + 15) & ~(size_t)15;
-    static constexpr size_t PLANE_BYTES = (size_t)RP * RP * sizeof(float2);
+    static constexpr size_t PLANE_BYTES = (size_t)ROWS * RP * sizeof(float2);
+    static_assert(RP >= padded_len<N>() && RP % 16 == 2, "row pitch");
+    static_assert(T == 8 && N % 128 == 0, "8 threads per row and column, rows in groups of 8");
     static constexpr size_t SMEM = TAB_BYTES + PLANE_BYTES;
     static_assert(NT == 1024, "one plane per 1024-thread CTA");
     static_assert(SMEM <= 225 * 1024, "plane does not fit shared memory");
@@ -82,9 +88,14 @@ __global__ void __launch_bounds__(PlaneGeom<N>::NT, 1) plane_kernel(const PlaneA
     asm volatile("griddepcontrol.wait;" ::: "memory");
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 
-    // row phase: row iy = tid / T, points iz = tr + T q; column phase: column iz = tid % N, points iy = tc + T q
-    const int row = tid / T, tr = tid % T;
-    const int col = tid % N, tc = tid / N;
+    // row phase: 8 threads per row (points iz = tr + T q); warp w holds rows 8(w/2) + 2(w%2) + {0, 1, 4, 5}
+    // (a half-warp: two rows four apart).  Column phase: 8 threads per column (points iy = tc + T q),
+    // warp w holds columns 4w .. 4w + 3.
+    const int warp = tid >> 5, lane = tid & 31;
+    const int tr = lane & 7;
+    const int row = 8 * (warp >> 1) + 2 * (warp & 1) + ((lane >> 4) & 1) + 4 * ((lane >> 3) & 1);
+    const int tc = lane & 7;
+    const int col = 4 * warp + (lane >> 3);
     C2<R>* sbr = plane + padp(row) * RP;
     C2<R>* sbc = plane + padp(col);
     const uint32_t ix = blockIdx.x;
@@ -140,10 +151,10 @@ __global__ void __launch_bounds__(PlaneGeom<N>::NT, 1) plane_kernel(const PlaneA
         __syncwarp();  // the row's exchange reads are done before its cells are overwritten
 #pragma unroll
         for (int q = 0; q < E; q++) rcell(q) = x[q];
-        __syncthreads();
+        __syncthreads();  // every row is in its cells
 #pragma unroll
         for (int q = 0; q < E; q++) x[q] = ccell(q);
-        fft<R, N, 0, false, RP, NT>(x, sbc, tc, stw, 0);
+        fft<R, N, 0, false, RP, 32>(x, sbc, tc, stw, 0);
         if (mode == 0) {
             const C2<R> kz = skz[col];
 #pragma unroll
@@ -154,11 +165,11 @@ __global__ void __launch_bounds__(PlaneGeom<N>::NT, 1) plane_kernel(const PlaneA
 #pragma unroll
             for (int q = 0; q < E; q++) x[q] = cscale(x[q], (sly[tc + T * q] + lz_) * inv);
         }
-        fft<R, N, 0, true, RP, NT>(x, sbc, tc, stw, 0);
-        __syncthreads();  // every column's exchange reads are done
+        fft<R, N, 0, true, RP, 32>(x, sbc, tc, stw, 0);
+        __syncwarp();  // the column's exchange reads are done before its cells are overwritten
 #pragma unroll
         for (int q = 0; q < E; q++) ccell(q) = x[q];
-        __syncthreads();
+        __syncthreads();  // every column is in its cells
 #pragma unroll
         for (int q = 0; q < E; q++) x[q] = rcell(q);
         fft<R, N, 0, true, 1, 32>(x, sbr, tr, stw, 0);
