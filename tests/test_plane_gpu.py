@@ -182,3 +182,36 @@ def test_plane_layout_with_enforced_phase_and_time_sliced_potential(cuda_device,
     kinds = [p["kind"] for p in e.profile_passes(1)]  # (steps further: after the comparison)
     assert kinds.count("plane") == 2, kinds
     e.close()
+
+
+def test_plane_layout_on_lattices_with_the_real_corrector_buffer(cuda_device, gpe_lib):
+    """Above 2^21 points the corrector keeps the real potential V' instead of exp(c3 V') (the Vstep3 plane
+    pass recomputes the phase): 256 x 128 x 128 with friction against the pencil passes after 20 steps and
+    against the oracle after one."""
+    shape, inter, qf, params, npart = (256, 128, 128), 0, 0.1, [0.04, 0.04, 0.06, 0.0], 1000.0
+    psi = configs.random_state(shape, seed=18, npart=npart, gamma=2.0)
+
+    def make(plane):
+        e = g.Engine(shape, inter, 1.0, 0.0, 0.05, npart, precision=g.FP32)
+        e.set_plane_passes(plane)
+        e.set_user_params(params)
+        e.set_quantum_friction_coeff(qf)
+        e.set_psi(0.0, psi)
+        return e
+
+    a = make(True)
+    assert [p["kind"] for p in a.profile_passes(1)].count("plane") == 2
+    a.close()
+    a, b = make(True), make(False)
+    a.evolve_qf(1)
+    o = oracle.Oracle(shape, inter, 1.0, 0.0, 0.05, npart, threads=8)
+    o.set_user_params(params)
+    o.set_quantum_friction_coeff(qf)
+    o.set_psi(0.0, psi)
+    o.evolve_qf(1)
+    assert rel(a.get_psi()[1], o.get_psi()[1]) <= 2e-5
+    a.evolve_qf(19)
+    b.evolve_qf(20)
+    assert rel(a.get_psi()[1], b.get_psi()[1]) <= 5e-5
+    a.close()
+    b.close()
