@@ -173,6 +173,34 @@ def test_time_dependent_user_hooks_match_oracle(kick_lib, case):
         x.close()
 
 
+@pytest.mark.parametrize("qf", [0.0, 0.1])
+def test_user_hooks_inside_the_plane_passes(kick_lib, qf):
+    """FP32 real time on 128 x 128 yz-planes runs the hooks inside the plane kernel (Vstep1 and the
+    corrector with the potential and functional at it and it + 1, gpe_modify_psi on psi_n): against the
+    oracle evaluating the same header, FP32 tolerances."""
+    shape, dt, t0 = (16, 128, 128), 0.05, 0.4
+    hooks = oracle.Hooks(oracle.build_hooks(KICK_HEADER, "test_kick", ["INTERACTIONS=-1"]))
+    psi = configs.random_state(shape, seed=34, npart=1.0, gamma=1.0)
+    o = oracle.Oracle(shape, -1, 1.0, 0.0, dt, 1.0, threads=8)
+    o.set_hooks(hooks)
+    o.set_user_params(KICK)
+    o.set_quantum_friction_coeff(qf)
+    o.set_psi(t0, psi)
+    e = g.Engine(shape, -1, 1.0, 0.0, dt, 1.0, precision=g.FP32, library=kick_lib)
+    e.set_user_params(KICK)
+    if qf:
+        e.set_quantum_friction_coeff(qf)
+    e.set_psi(t0, psi)
+    for steps, tol in ((1, 2e-5), (9, 1e-4)):
+        o.evolve_qf(steps)
+        e.evolve_qf(steps)
+        assert rel(e.get_psi()[1], o.get_psi()[1]) <= tol, (steps, rel(e.get_psi()[1], o.get_psi()[1]))
+    # (the library holds 16- and 32-point pencils only: the plane passes carry every y and z transform)
+    kinds = [p["kind"] for p in e.profile_passes(1)]
+    assert kinds.count("plane") == 2 and len(kinds) == 4, kinds
+    e.close()
+
+
 DEFAULT_CASES = [
     # shape, alpha, beta, dt, qf
     ((16, 32, 32), 1.0, 0.0, 0.05, 0.1),
