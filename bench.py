@@ -708,12 +708,13 @@ def main():
         extras["fp64_plain"] = {"value": 3 * b64 / t64, "unit": "steps/s", "dtype": "f64",
                                 "roofline": fp64_rooflines(3 * b64 / t64, int(np.prod(w.shape)),
                                                            measured_fp64_peak(), qf=w.qf != 0.0)}
-        # the binding unit, counted by ncu on this workload's seven FP64 passes (one steady step):
-        # every DADD/DMUL/DFMA, where fp64_alu counts nominal FFT flops
-        extras["fp64_plain"]["roofline"]["fp64_pipe"] = {
-            "active_frac": 0.83, "per_pass": [0.819, 0.844, 0.835, 0.830, 0.832, 0.835, 0.842],
-            "how": "ncu sm__pipe_fp64_cycles_active.avg.pct_of_peak_sustained_active, one steady step of "
-                   "the 128^3 FP64 friction schedule (pass_kernel_fp64_pipe_128_ufg_qf.md)"}
+        # the binding unit, counted by ncu on this workload's seven FP64 passes (one steady step of the
+        # 128^3 friction schedule): every DADD/DMUL/DFMA, where fp64_alu counts nominal FFT flops
+        if tuple(w.shape) == (128, 128, 128) and w.qf != 0.0:
+            extras["fp64_plain"]["roofline"]["fp64_pipe"] = {
+                "active_frac": 0.83, "per_pass": [0.819, 0.844, 0.835, 0.830, 0.832, 0.835, 0.842],
+                "how": "ncu sm__pipe_fp64_cycles_active.avg.pct_of_peak_sustained_active, one steady step "
+                       "of the 128^3 FP64 friction schedule (pass_kernel_fp64_pipe_128_ufg_qf.md)"}
         e64.close()
         # FP32 energy and density error against the FP64 form over the workload's full run
         a = make_engine(w, psi, g.FP32)
