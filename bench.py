@@ -36,6 +36,9 @@ sys.path.insert(0, ROOT)
 B_ALG = {  # algorithmic bytes per grid point per step (8 S + S + 4 s_r, + 4 S with quantum friction)
     ("fp32", True): 120, ("fp32", False): 88, ("fp64", True): 240, ("fp64", False): 176,
 }
+# warp instructions of one GPE step of the 128^3 FP32 friction step in the yz-plane layout (ncu
+# smsp__inst_executed.sum over its four launches, profiles/plane_and_pass_kernel_issue_bound_128_fp32_ufg_qf.md)
+INST_PER_STEP_128_PLANE = 59.9e6
 
 
 def peaks():
@@ -781,6 +784,18 @@ def main():
         top = max(per_pass, key=lambda p: p["share"])
         traffic, traffic_how = traffic_from_profiles(w.shape[0])
         clk_s = clk.summary()
+        # the unit that binds the L2-resident 128^3 step: instruction issue (one warp instruction per
+        # scheduler per cycle, four schedulers per SM, at the SM clock sampled during the timed region)
+        issue = None
+        if tuple(w.shape) == (128, 128, 128) and w.qf != 0.0 and any(p["kind"] == "plane" for p in passes):
+            sms = torch.cuda.get_device_properties(local).multi_processor_count
+            mhz = clk_s.get("sm_mhz") or clk_s.get("sm_max_mhz") or 2070.0
+            peak_inst = sms * 4 * mhz * 1e6
+            ach_inst = INST_PER_STEP_128_PLANE / gpe_step_s
+            issue = {"unit": "warp instructions/s", "achieved": ach_inst, "peak": peak_inst,
+                     "frac": ach_inst / peak_inst, "inst_per_gpe_step": INST_PER_STEP_128_PLANE,
+                     "how": f"ncu instruction count per GPE step / timed GPE step; peak = {sms} SMs x 4 "
+                            f"schedulers x {mhz:.0f} MHz (plane_and_pass_kernel_issue_bound_128_fp32_ufg_qf.md)"}
         line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * t32 / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
@@ -794,7 +809,8 @@ def main():
                                       f"stream); peak {kind}; traffic = ncu DRAM bytes per GPE step",
                              "per_pass": per_pass,
                              "top_pass": top,
-                             "per_pass_event_sum_us": round(1e3 * ev_total, 2)},
+                             "per_pass_event_sum_us": round(1e3 * ev_total, 2),
+                             "issue": issue},
                 "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": 16 * n,
                         "d2h_bytes_per_step": 16 * n},
                 "gpu_launches": launches, "clocks": clk_s, "autotune": tuned}
