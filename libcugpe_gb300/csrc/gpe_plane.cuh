@@ -175,13 +175,24 @@ __global__ void __launch_bounds__(PlaneGeom<N>::NT, 1) plane_kernel(const PlaneA
         fft<R, N, 0, true, 1, 32>(x, sbr, tr, stw, 0);
     };
 
-    if (a.flags & F_LAP) {
-        // y + z Laplacian of the input only (the first step after psi changed)
-        pair2d(1);
+    // The transform pairs of the pass run in one rolled loop, so the four transforms appear once in the
+    // instruction stream: k = 0 is the step's pair (kinetic, then the POST op and the store) or, with
+    // F_LAP, the Laplacian of the input alone; k = 1 the Laplacian of the result (F_LAP_OUT).
+    const bool lap_only = (a.flags & F_LAP) != 0;
+#pragma unroll 1
+    for (int k = 0; k < 2; k++) {
+        if (k == 1) {
+            if (lap_only || !(a.flags & F_LAP_OUT)) break;
+            __syncthreads();  // the plane's cells are free again
+        }
+        const int mode = (k == 1 || lap_only) ? 1 : 0;
+        if (mode == 1 || (a.flags & F_KIN)) pair2d(mode);
+        if (mode == 1) {
+            // y + z Laplacian (of the input with F_LAP, of the result with F_LAP_OUT)
 #pragma unroll
-        for (int q = 0; q < E; q++) a.lap[at(q)] = x[q];
-    } else {
-        if (a.flags & F_KIN) pair2d(0);
+            for (int q = 0; q < E; q++) a.lap[at(q)] = x[q];
+            continue;
+        }
 
         // -------------------------------------------------------- POST (row cells)
         if (a.post == POST_PART12) {
@@ -240,13 +251,6 @@ __global__ void __launch_bounds__(PlaneGeom<N>::NT, 1) plane_kernel(const PlaneA
         if (a.flags & F_STORE) {
 #pragma unroll
             for (int q = 0; q < E; q++) a.out[at(q)] = x[q];
-        }
-        if (a.flags & F_LAP_OUT) {
-            // y + z Laplacian of the result, for the next step's friction potential
-            __syncthreads();  // the plane's cells are free again
-            pair2d(1);
-#pragma unroll
-            for (int q = 0; q < E; q++) a.lap[at(q)] = x[q];
         }
     }
 
