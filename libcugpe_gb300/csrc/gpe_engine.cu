@@ -1078,7 +1078,8 @@ struct Control {
     double2* bufA = nullptr;
     double2* bufC = nullptr;
     double* Vn = nullptr;
-    double* W = nullptr;
+    double2* Eph = nullptr;      // exp(c3 V_n) of the step being reversed (the forward recompute's factor)
+    double2* Fph = nullptr;      // exp(c3 W), W the corrector's averaged potential
     double* Wbar = nullptr;
     double* Vbar = nullptr;
     double2* ktc = nullptr;      // conjugate kinetic tables, nx + ny + nz
@@ -1152,32 +1153,38 @@ __global__ void k_ctl_seed(const double2* t, double2* bar, size_t n, double2 o) 
     }
 }
 
-// V = Vext(n) + g|psi|^2 -> Vn ; A = exp(c3 V) psi -> bufA
-__global__ void k_ctl_fw1(CtlArgs a, unsigned it, const double2* psi, double* Vn, double2* A) {
+// The phase factors E = exp(c3 V) and F = exp(c3 W) are kept from the forward recompute for the reverse
+// kernels (the same bits as recomputing them; five FP64 sincos per point and step fewer).
+
+// V = Vext(n) + g|psi|^2 -> Vn ; E -> Eph ; A = E psi -> bufA
+__global__ void k_ctl_fw1(CtlArgs a, unsigned it, const double2* psi, double* Vn, double2* Eph, double2* A) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < a.n; i += (size_t)gridDim.x * blockDim.x) {
         const double2 p = psi[i];
         const double V = ctl_vext(a, i, it) + a.g * (p.x * p.x + p.y * p.y);
         Vn[i] = V;
-        A[i] = cmul(p, ctl_phase(a.c3y, V));
+        const double2 E = ctl_phase(a.c3y, V);
+        Eph[i] = E;
+        A[i] = cmul(p, E);
     }
 }
 
-// P = E B ; W = (V + Vext(n+1) + g|P|^2)/2 -> W ; C = exp(c3 W) psi -> bufC
-__global__ void k_ctl_fw2(CtlArgs a, unsigned it, const double2* psi, const double* Vn, const double2* B, double* W,
-                          double2* C) {
+// P = E B ; W = (V + Vext(n+1) + g|P|^2)/2 ; F = exp(c3 W) -> Fph ; C = F psi -> bufC
+__global__ void k_ctl_fw2(CtlArgs a, unsigned it, const double2* psi, const double* Vn, const double2* Eph,
+                          const double2* B, double2* Fph, double2* C) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < a.n; i += (size_t)gridDim.x * blockDim.x) {
         const double V = Vn[i];
-        const double2 P = cmul(B[i], ctl_phase(a.c3y, V));
+        const double2 P = cmul(B[i], Eph[i]);
         const double w = 0.5 * ((V + ctl_vext(a, i, it + 1)) + a.g * (P.x * P.x + P.y * P.y));
-        W[i] = w;
-        C[i] = cmul(psi[i], ctl_phase(a.c3y, w));
+        const double2 F = ctl_phase(a.c3y, w);
+        Fph[i] = F;
+        C[i] = cmul(psi[i], F);
     }
 }
 
 // psi_{n+1} = F D ; Wbar = Re(c3 psi_{n+1} conj(bar)) ; D_bar = conj(F) bar -> bufC
-__global__ void k_ctl_bw1(CtlArgs a, const double* W, double2* CD, const double2* bar, double* Wbar) {
+__global__ void k_ctl_bw1(CtlArgs a, const double2* Fph, double2* CD, const double2* bar, double* Wbar) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < a.n; i += (size_t)gridDim.x * blockDim.x) {
-        const double2 F = ctl_phase(a.c3y, W[i]);
+        const double2 F = Fph[i];
         const double2 nb = bar[i];
         const double2 pn = cmul(F, CD[i]);
         Wbar[i] = ctl_vbar(a.c3y, pn, nb);
@@ -1188,21 +1195,22 @@ __global__ void k_ctl_bw1(CtlArgs a, const double* W, double2* CD, const double2
 // with C_bar in bufC: bar = conj(F) C_bar ; W_bar += Re(c3 C conj(C_bar)) ;
 // V_bar = W_bar/2 ; Vext(n+1)_bar = W_bar/2 (projected) ; P = E B ;
 // P_bar = g W_bar P ; B_bar = conj(E) P_bar -> bufA ; V_bar += Re(c3 P conj(P_bar))
-__global__ void __launch_bounds__(kCtlThreads) k_ctl_bw2(CtlArgs a, const double2* psi, const double* Vn, const double* W,
-                                                        const double* Wbar, const double2* Cbar, double2* AB, double* Vbar,
-                                                        double2* bar, const double* basis, int nbasis, double* part) {
+__global__ void __launch_bounds__(kCtlThreads) k_ctl_bw2(CtlArgs a, const double2* psi, const double2* Eph,
+                                                        const double2* Fph, const double* Wbar, const double2* Cbar,
+                                                        double2* AB, double* Vbar, double2* bar, const double* basis,
+                                                        int nbasis, double* part) {
     __shared__ double sp[kCtlMaxBasis][kCtlThreads / 32];
     // per-basis partial projections in registers: every index below is a compile-time constant
     double acc[kCtlMaxBasis];
 #pragma unroll
     for (int k = 0; k < kCtlMaxBasis; k++) acc[k] = 0.0;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < a.n; i += (size_t)gridDim.x * blockDim.x) {
-        const double2 F = ctl_phase(a.c3y, W[i]);
+        const double2 F = Fph[i];
         const double2 cb = Cbar[i];
         const double2 C = cmul(F, psi[i]);
         bar[i] = cmulc(cb, F);
         const double wb = Wbar[i] + ctl_vbar(a.c3y, C, cb);
-        const double2 E = ctl_phase(a.c3y, Vn[i]);
+        const double2 E = Eph[i];
         const double2 P = cmul(AB[i], E);
         const double2 Pb = make_double2(a.g * wb * P.x, a.g * wb * P.y);
         AB[i] = cmulc(Pb, E);
@@ -1230,7 +1238,7 @@ __global__ void __launch_bounds__(kCtlThreads) k_ctl_bw2(CtlArgs a, const double
 
 // with A_bar in bufA: bar += conj(E) A_bar ; V_bar += Re(c3 A conj(A_bar)) ;
 // Vext(n)_bar = V_bar (projected) ; bar += 2 g V_bar psi
-__global__ void __launch_bounds__(kCtlThreads) k_ctl_bw3(CtlArgs a, const double2* psi, const double* Vn,
+__global__ void __launch_bounds__(kCtlThreads) k_ctl_bw3(CtlArgs a, const double2* psi, const double2* Eph,
                                                         const double2* Abar, const double* Vbar, double2* bar,
                                                         const double* basis, int nbasis, double* part) {
     __shared__ double sp[kCtlMaxBasis][kCtlThreads / 32];
@@ -1239,7 +1247,7 @@ __global__ void __launch_bounds__(kCtlThreads) k_ctl_bw3(CtlArgs a, const double
 #pragma unroll
     for (int k = 0; k < kCtlMaxBasis; k++) acc[k] = 0.0;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < a.n; i += (size_t)gridDim.x * blockDim.x) {
-        const double2 E = ctl_phase(a.c3y, Vn[i]);
+        const double2 E = Eph[i];
         const double2 p = psi[i];
         const double2 A = cmul(E, p);
         const double2 ab = Abar[i];
@@ -1406,19 +1414,19 @@ static int ctl_backward(Control* c, double2 o, double* grad_host) {
             const unsigned it = (unsigned)(j * c->ck + i);
             const double2* psi = c->seg + (size_t)i * n;
             GPE_RC(ctl_fill(c, it));
-            k_ctl_fw1<<<1024, 256, 0, e->st>>>(a, it, psi, c->Vn, c->bufA);
+            k_ctl_fw1<<<1024, 256, 0, e->st>>>(a, it, psi, c->Vn, c->Eph, c->bufA);
             GPE_RC(ctl_kinetic(c, c->bufA, 0));
-            k_ctl_fw2<<<1024, 256, 0, e->st>>>(a, it, psi, c->Vn, c->bufA, c->W, c->bufC);
+            k_ctl_fw2<<<1024, 256, 0, e->st>>>(a, it, psi, c->Vn, c->Eph, c->bufA, c->Fph, c->bufC);
             GPE_RC(ctl_kinetic(c, c->bufC, 0));
-            k_ctl_bw1<<<1024, 256, 0, e->st>>>(a, c->W, c->bufC, c->bar, c->Wbar);
+            k_ctl_bw1<<<1024, 256, 0, e->st>>>(a, c->Fph, c->bufC, c->bar, c->Wbar);
             GPE_RC(ctl_kinetic(c, c->bufC, 1));
-            k_ctl_bw2<<<kCtlBlocks, kCtlThreads, 0, e->st>>>(a, psi, c->Vn, c->W, c->Wbar, c->bufC, c->bufA, c->Vbar,
+            k_ctl_bw2<<<kCtlBlocks, kCtlThreads, 0, e->st>>>(a, psi, c->Eph, c->Fph, c->Wbar, c->bufC, c->bufA, c->Vbar,
                                                           c->bar, c->basis, c->nbasis, c->part);
             int s1 = (int)((it + 1) / (unsigned)c->sps);
             if (s1 >= c->nslices) s1 = c->nslices - 1;
             k_ctl_accumulate<<<1, kCtlMaxBasis, 0, e->st>>>(c->part, kCtlBlocks, c->nbasis, c->grad + (size_t)s1 * c->nbasis);
             GPE_RC(ctl_kinetic(c, c->bufA, 1));
-            k_ctl_bw3<<<kCtlBlocks, kCtlThreads, 0, e->st>>>(a, psi, c->Vn, c->bufA, c->Vbar, c->bar, c->basis,
+            k_ctl_bw3<<<kCtlBlocks, kCtlThreads, 0, e->st>>>(a, psi, c->Eph, c->bufA, c->Vbar, c->bar, c->basis,
                                                           c->nbasis, c->part);
             int s0 = (int)(it / (unsigned)c->sps);
             if (s0 >= c->nslices) s0 = c->nslices - 1;
@@ -1440,7 +1448,7 @@ static void ctl_release(Control* c) {
         c->e->version++;
     }
     cudaFree(c->basis); cudaFree(c->controls); cudaFree(c->fields); cudaFree(c->target); cudaFree(c->ckpt);
-    cudaFree(c->seg); cudaFree(c->bar); cudaFree(c->bufA); cudaFree(c->bufC); cudaFree(c->Vn); cudaFree(c->W);
+    cudaFree(c->seg); cudaFree(c->bar); cudaFree(c->bufA); cudaFree(c->bufC); cudaFree(c->Vn); cudaFree(c->Eph); cudaFree(c->Fph);
     cudaFree(c->Wbar); cudaFree(c->Vbar); cudaFree(c->ktc); cudaFree(c->part); cudaFree(c->grad); cudaFree(c->ovl);
 }
 
@@ -2296,7 +2304,8 @@ int gpe_gb_control_create(gpe_gb_control** out, gpe_gb_engine* h, int nbasis, co
     alloc((void**)&c->bufA, sizeof(double2) * n);
     alloc((void**)&c->bufC, sizeof(double2) * n);
     alloc((void**)&c->Vn, sizeof(double) * n);
-    alloc((void**)&c->W, sizeof(double) * n);
+    alloc((void**)&c->Eph, sizeof(double2) * n);
+    alloc((void**)&c->Fph, sizeof(double2) * n);
     alloc((void**)&c->Wbar, sizeof(double) * n);
     alloc((void**)&c->Vbar, sizeof(double) * n);
     alloc((void**)&c->ktc, sizeof(double2) * (e->n3[0] + e->n3[1] + e->n3[2]));
