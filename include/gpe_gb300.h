@@ -210,7 +210,9 @@ long long gpe_gb_batch_kernel_launches(const gpe_gb_batch* b);
  * basis: nbasis real fields (nbasis <= 32), lattice units; controls:
  * nslices*nbasis, lattice units, row s = slice.  While the problem exists it
  * owns the engine's time-sliced potential and uses the engine's psi as
- * scratch. */
+ * scratch.  Device memory: about (5 checkpoint_every + nsteps/checkpoint_every
+ * + nbasis/2 + 8) complex128 fields (a segment's states and per-step
+ * intermediates, the checkpoints, the basis). */
 typedef struct gpe_gb_control gpe_gb_control;
 int gpe_gb_control_create(gpe_gb_control** out, gpe_gb_engine* engine, int nbasis, const double* basis, int nslices,
                           int steps_per_slice, int nsteps, int checkpoint_every, const double* psi_target);

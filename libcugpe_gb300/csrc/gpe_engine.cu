@@ -1075,11 +1075,12 @@ struct Control {
     int nckpt = 0;
     double2* seg = nullptr;      // [ck][n] states of the segment being reversed
     double2* bar = nullptr;      // cotangent of psi
-    double2* bufA = nullptr;
-    double2* bufC = nullptr;
+    // per step of the segment being reversed ([ck][n] each), from the forward recompute:
+    double2* stE = nullptr;      // E = exp(c3 V_n)
+    double2* stF = nullptr;      // F = exp(c3 W), W the corrector's averaged potential
+    double2* stB = nullptr;      // B = K E psi_n (the predictor before its second factor), later its cotangent
+    double2* stD = nullptr;      // D = K F psi_n (psi_{n+1} = F D), later its cotangent
     double* Vn = nullptr;
-    double2* Eph = nullptr;      // exp(c3 V_n) of the step being reversed (the forward recompute's factor)
-    double2* Fph = nullptr;      // exp(c3 W), W the corrector's averaged potential
     double* Wbar = nullptr;
     double* Vbar = nullptr;
     double2* ktc = nullptr;      // conjugate kinetic tables, nx + ny + nz
@@ -1153,10 +1154,11 @@ __global__ void k_ctl_seed(const double2* t, double2* bar, size_t n, double2 o) 
     }
 }
 
-// The phase factors E = exp(c3 V) and F = exp(c3 W) are kept from the forward recompute for the reverse
-// kernels (the same bits as recomputing them; five FP64 sincos per point and step fewer).
+// The forward recompute of a segment runs the step as these kernels and keeps, per step, the phase
+// factors E = exp(c3 V) and F = exp(c3 W) and the kinetic results B and D, so the reverse sweep needs
+// no second recompute (and no FP64 sincos).
 
-// V = Vext(n) + g|psi|^2 -> Vn ; E -> Eph ; A = E psi -> bufA
+// V = Vext(n) + g|psi|^2 -> Vn ; E -> Eph ; A = E psi -> A
 __global__ void k_ctl_fw1(CtlArgs a, unsigned it, const double2* psi, double* Vn, double2* Eph, double2* A) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < a.n; i += (size_t)gridDim.x * blockDim.x) {
         const double2 p = psi[i];
@@ -1168,7 +1170,7 @@ __global__ void k_ctl_fw1(CtlArgs a, unsigned it, const double2* psi, double* Vn
     }
 }
 
-// P = E B ; W = (V + Vext(n+1) + g|P|^2)/2 ; F = exp(c3 W) -> Fph ; C = F psi -> bufC
+// P = E B ; W = (V + Vext(n+1) + g|P|^2)/2 ; F = exp(c3 W) -> Fph ; C = F psi -> C
 __global__ void k_ctl_fw2(CtlArgs a, unsigned it, const double2* psi, const double* Vn, const double2* Eph,
                           const double2* B, double2* Fph, double2* C) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < a.n; i += (size_t)gridDim.x * blockDim.x) {
@@ -1181,7 +1183,13 @@ __global__ void k_ctl_fw2(CtlArgs a, unsigned it, const double2* psi, const doub
     }
 }
 
-// psi_{n+1} = F D ; Wbar = Re(c3 psi_{n+1} conj(bar)) ; D_bar = conj(F) bar -> bufC
+// psi_{n+1} = F D (the next state of the recompute)
+__global__ void k_ctl_next(const double2* Fph, const double2* D, double2* out, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = cmul(Fph[i], D[i]);
+}
+
+// psi_{n+1} = F D ; Wbar = Re(c3 psi_{n+1} conj(bar)) ; D_bar = conj(F) bar -> D
 __global__ void k_ctl_bw1(CtlArgs a, const double2* Fph, double2* CD, const double2* bar, double* Wbar) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < a.n; i += (size_t)gridDim.x * blockDim.x) {
         const double2 F = Fph[i];
@@ -1192,9 +1200,9 @@ __global__ void k_ctl_bw1(CtlArgs a, const double2* Fph, double2* CD, const doub
     }
 }
 
-// with C_bar in bufC: bar = conj(F) C_bar ; W_bar += Re(c3 C conj(C_bar)) ;
+// with C_bar in D: bar = conj(F) C_bar ; W_bar += Re(c3 C conj(C_bar)) ;
 // V_bar = W_bar/2 ; Vext(n+1)_bar = W_bar/2 (projected) ; P = E B ;
-// P_bar = g W_bar P ; B_bar = conj(E) P_bar -> bufA ; V_bar += Re(c3 P conj(P_bar))
+// P_bar = g W_bar P ; B_bar = conj(E) P_bar -> B ; V_bar += Re(c3 P conj(P_bar))
 __global__ void __launch_bounds__(kCtlThreads) k_ctl_bw2(CtlArgs a, const double2* psi, const double2* Eph,
                                                         const double2* Fph, const double* Wbar, const double2* Cbar,
                                                         double2* AB, double* Vbar, double2* bar, const double* basis,
@@ -1236,7 +1244,7 @@ __global__ void __launch_bounds__(kCtlThreads) k_ctl_bw2(CtlArgs a, const double
     }
 }
 
-// with A_bar in bufA: bar += conj(E) A_bar ; V_bar += Re(c3 A conj(A_bar)) ;
+// with A_bar in B: bar += conj(E) A_bar ; V_bar += Re(c3 A conj(A_bar)) ;
 // Vext(n)_bar = V_bar (projected) ; bar += 2 g V_bar psi
 __global__ void __launch_bounds__(kCtlThreads) k_ctl_bw3(CtlArgs a, const double2* psi, const double2* Eph,
                                                         const double2* Abar, const double* Vbar, double2* bar,
@@ -1402,36 +1410,48 @@ static int ctl_backward(Control* c, double2 o, double* grad_host) {
     GPE_CK(cudaMemsetAsync(c->grad, 0, sizeof(double) * c->nslices * c->nbasis, e->st));
     k_ctl_seed<<<1024, 256, 0, e->st>>>(c->target, c->bar, n, o);
     for (int j = nseg - 1; j >= 0; j--) {
-        // recompute the segment's states forward from its checkpoint
-        GPE_CK(cudaMemcpyAsync(e->psi, c->ckpt + (size_t)j * n, sizeof(double2) * n, cudaMemcpyDeviceToDevice, e->st));
-        e->it = (unsigned)(j * c->ck);
-        GPE_RC(set_state(e, e->it, 1.0));
+        // recompute the segment forward from its checkpoint, keeping each step's intermediates
+        GPE_CK(cudaMemcpyAsync(c->seg, c->ckpt + (size_t)j * n, sizeof(double2) * n, cudaMemcpyDeviceToDevice, e->st));
         for (int i = 0; i < c->ck; i++) {
-            GPE_CK(cudaMemcpyAsync(c->seg + (size_t)i * n, e->psi, sizeof(double2) * n, cudaMemcpyDeviceToDevice, e->st));
-            GPE_RC(ctl_steps(c, 1));
+            const unsigned it = (unsigned)(j * c->ck + i);
+            const double2* psi = c->seg + (size_t)i * n;
+            double2* E = c->stE + (size_t)i * n;
+            double2* F = c->stF + (size_t)i * n;
+            double2* B = c->stB + (size_t)i * n;
+            double2* D = c->stD + (size_t)i * n;
+            GPE_RC(ctl_fill(c, it));
+            k_ctl_fw1<<<1024, 256, 0, e->st>>>(a, it, psi, c->Vn, E, B);
+            GPE_RC(ctl_kinetic(c, B, 0));
+            k_ctl_fw2<<<1024, 256, 0, e->st>>>(a, it, psi, c->Vn, E, B, F, D);
+            GPE_RC(ctl_kinetic(c, D, 0));
+            e->launches += 2;
+            if (i + 1 < c->ck) {
+                k_ctl_next<<<1024, 256, 0, e->st>>>(F, D, c->seg + (size_t)(i + 1) * n, n);
+                e->launches++;
+            }
+            GPE_CK(cudaGetLastError());
         }
         for (int i = c->ck - 1; i >= 0; i--) {
             const unsigned it = (unsigned)(j * c->ck + i);
             const double2* psi = c->seg + (size_t)i * n;
-            GPE_RC(ctl_fill(c, it));
-            k_ctl_fw1<<<1024, 256, 0, e->st>>>(a, it, psi, c->Vn, c->Eph, c->bufA);
-            GPE_RC(ctl_kinetic(c, c->bufA, 0));
-            k_ctl_fw2<<<1024, 256, 0, e->st>>>(a, it, psi, c->Vn, c->Eph, c->bufA, c->Fph, c->bufC);
-            GPE_RC(ctl_kinetic(c, c->bufC, 0));
-            k_ctl_bw1<<<1024, 256, 0, e->st>>>(a, c->Fph, c->bufC, c->bar, c->Wbar);
-            GPE_RC(ctl_kinetic(c, c->bufC, 1));
-            k_ctl_bw2<<<kCtlBlocks, kCtlThreads, 0, e->st>>>(a, psi, c->Eph, c->Fph, c->Wbar, c->bufC, c->bufA, c->Vbar,
+            const double2* E = c->stE + (size_t)i * n;
+            const double2* F = c->stF + (size_t)i * n;
+            double2* B = c->stB + (size_t)i * n;
+            double2* D = c->stD + (size_t)i * n;
+            k_ctl_bw1<<<1024, 256, 0, e->st>>>(a, F, D, c->bar, c->Wbar);
+            GPE_RC(ctl_kinetic(c, D, 1));
+            k_ctl_bw2<<<kCtlBlocks, kCtlThreads, 0, e->st>>>(a, psi, E, F, c->Wbar, D, B, c->Vbar,
                                                           c->bar, c->basis, c->nbasis, c->part);
             int s1 = (int)((it + 1) / (unsigned)c->sps);
             if (s1 >= c->nslices) s1 = c->nslices - 1;
             k_ctl_accumulate<<<1, kCtlMaxBasis, 0, e->st>>>(c->part, kCtlBlocks, c->nbasis, c->grad + (size_t)s1 * c->nbasis);
-            GPE_RC(ctl_kinetic(c, c->bufA, 1));
-            k_ctl_bw3<<<kCtlBlocks, kCtlThreads, 0, e->st>>>(a, psi, c->Eph, c->bufA, c->Vbar, c->bar, c->basis,
+            GPE_RC(ctl_kinetic(c, B, 1));
+            k_ctl_bw3<<<kCtlBlocks, kCtlThreads, 0, e->st>>>(a, psi, E, B, c->Vbar, c->bar, c->basis,
                                                           c->nbasis, c->part);
             int s0 = (int)(it / (unsigned)c->sps);
             if (s0 >= c->nslices) s0 = c->nslices - 1;
             k_ctl_accumulate<<<1, kCtlMaxBasis, 0, e->st>>>(c->part, kCtlBlocks, c->nbasis, c->grad + (size_t)s0 * c->nbasis);
-            e->launches += 8;
+            e->launches += 5;
             GPE_CK(cudaGetLastError());
         }
     }
@@ -1448,7 +1468,7 @@ static void ctl_release(Control* c) {
         c->e->version++;
     }
     cudaFree(c->basis); cudaFree(c->controls); cudaFree(c->fields); cudaFree(c->target); cudaFree(c->ckpt);
-    cudaFree(c->seg); cudaFree(c->bar); cudaFree(c->bufA); cudaFree(c->bufC); cudaFree(c->Vn); cudaFree(c->Eph); cudaFree(c->Fph);
+    cudaFree(c->seg); cudaFree(c->bar); cudaFree(c->stE); cudaFree(c->stF); cudaFree(c->stB); cudaFree(c->stD); cudaFree(c->Vn);
     cudaFree(c->Wbar); cudaFree(c->Vbar); cudaFree(c->ktc); cudaFree(c->part); cudaFree(c->grad); cudaFree(c->ovl);
 }
 
@@ -2301,11 +2321,8 @@ int gpe_gb_control_create(gpe_gb_control** out, gpe_gb_engine* h, int nbasis, co
     alloc((void**)&c->ckpt, sizeof(double2) * n * c->nckpt);
     alloc((void**)&c->seg, sizeof(double2) * n * c->ck);
     alloc((void**)&c->bar, sizeof(double2) * n);
-    alloc((void**)&c->bufA, sizeof(double2) * n);
-    alloc((void**)&c->bufC, sizeof(double2) * n);
     alloc((void**)&c->Vn, sizeof(double) * n);
-    alloc((void**)&c->Eph, sizeof(double2) * n);
-    alloc((void**)&c->Fph, sizeof(double2) * n);
+    for (double2** p : {&c->stE, &c->stF, &c->stB, &c->stD}) alloc((void**)p, sizeof(double2) * n * c->ck);
     alloc((void**)&c->Wbar, sizeof(double) * n);
     alloc((void**)&c->Vbar, sizeof(double) * n);
     alloc((void**)&c->ktc, sizeof(double2) * (e->n3[0] + e->n3[1] + e->n3[2]));
