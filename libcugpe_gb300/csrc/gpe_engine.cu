@@ -1060,8 +1060,9 @@ namespace gpe {
 // Cotangents z_bar = dL/dRe z + i dL/dIm z; for w = a z, z_bar = conj(a) w_bar;
 // for w = exp(c3 V) z with real V, V_bar += Re(c3 w conj(w_bar)); for rho = |z|^2,
 // z_bar += 2 rho_bar z; K^dagger is the kinetic pass with the conjugate table.
-// Forward states are kept at checkpoints every `ck` steps and each segment is
-// recomputed forward before its reverse sweep.
+// Forward states are kept at checkpoints every `ck` steps; each segment is
+// recomputed forward as the step above (keeping psi_n, E, F, B and D of every
+// step) before its reverse sweep.
 
 struct Control {
     Engine* e = nullptr;
@@ -1158,7 +1159,7 @@ __global__ void k_ctl_seed(const double2* t, double2* bar, size_t n, double2 o) 
 // factors E = exp(c3 V) and F = exp(c3 W) and the kinetic results B and D, so the reverse sweep needs
 // no second recompute (and no FP64 sincos).
 
-// V = Vext(n) + g|psi|^2 -> Vn ; E -> Eph ; A = E psi -> A
+// V = Vext(n) + g|psi|^2 -> Vn ; E -> Eph ; A = E psi -> A (the kinetic pass makes it B)
 __global__ void k_ctl_fw1(CtlArgs a, unsigned it, const double2* psi, double* Vn, double2* Eph, double2* A) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < a.n; i += (size_t)gridDim.x * blockDim.x) {
         const double2 p = psi[i];
@@ -1170,7 +1171,7 @@ __global__ void k_ctl_fw1(CtlArgs a, unsigned it, const double2* psi, double* Vn
     }
 }
 
-// P = E B ; W = (V + Vext(n+1) + g|P|^2)/2 ; F = exp(c3 W) -> Fph ; C = F psi -> C
+// P = E B ; W = (V + Vext(n+1) + g|P|^2)/2 ; F = exp(c3 W) -> Fph ; C = F psi -> C (then D)
 __global__ void k_ctl_fw2(CtlArgs a, unsigned it, const double2* psi, const double* Vn, const double2* Eph,
                           const double2* B, double2* Fph, double2* C) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < a.n; i += (size_t)gridDim.x * blockDim.x) {
