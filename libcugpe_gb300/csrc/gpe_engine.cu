@@ -413,6 +413,7 @@ static Phys<R> make_phys(const Engine* e) {
     p.gamma = (R)e->gamma;
     p.c3x = (R)c3x;
     p.c3y = (R)c3y;
+    p.c3y_pi = (R)(c3y / M_PI);
     p.c_bec = (R)(4 * M_PI * e->up[3]);
     p.a_scat = (R)e->up[3];
     p.qf_eps = (R)1.0e-12;

@@ -32,6 +32,7 @@ struct Phys {
     int phase_mode;   // which parts of c3 are non-zero
     R gamma;          // 1 particles, 2 dimers
     R c3x, c3y;       // c3 = Gamma dt/2 / (-beta + i alpha)   (dev/gpe_engine.cu:177-181)
+    R c3y_pi;         // c3y / pi (the rotation angle in units of pi)
     R c_bec;          // (4 pi) a, contact BEC mean field
     R a_scat;         // scattering length (user param A_SCAT)
     R qf_eps;         // 1e-12 (dev/gpe_engine.cuh:53)
@@ -46,6 +47,8 @@ __device__ __forceinline__ double gexp(double x) { return exp(x); }
 __device__ __forceinline__ float gexp(float x) { return expf(x); }
 __device__ __forceinline__ void gsincos(double x, double* s, double* c) { sincos(x, s, c); }
 __device__ __forceinline__ void gsincos(float x, float* s, float* c) { sincosf(x, s, c); }
+__device__ __forceinline__ void gsincospi(double x, double* s, double* c) { sincospi(x, s, c); }
+__device__ __forceinline__ void gsincospi(float x, float* s, float* c) { sincospif(x, s, c); }
 __device__ __forceinline__ double gcbrt(double x) { return cbrt(x); }
 __device__ __forceinline__ float gcbrt(float x) { return cbrtf(x); }
 __device__ __forceinline__ double gpow(double x, double y) { return pow(x, y); }
@@ -89,18 +92,26 @@ __device__ __forceinline__ double EDF(const Phys<double>& p, double rho) {
     return 0.6 * eF * rho * XI * (XI + x) / (XI + x * (1.0 + CT) + 3.0 * M_PI * XI * x * x) - rho / (2.0 * a * a);
 }
 
+// sin and cos of the rotation angle c3y V.  FP32: sincospif of the angle in units of pi (its argument
+// reduction is exact and short, and the kernels keep no local-memory reduction table; measured 2% faster
+// at 128^3, FP32 rounding of the angle as before); FP64: sincos (sincospi measured slower there).
+template <typename R> __device__ __forceinline__ void rotation(const Phys<R>& p, R V, R* s, R* c) {
+    if constexpr (sizeof(R) == 4) gsincospi(p.c3y_pi * V, s, c);
+    else gsincos(p.c3y * V, s, c);
+}
+
 // exp(c3 * V)
 template <typename R> __device__ __forceinline__ C2<R> phase(const Phys<R>& p, R V) {
     C2<R> e;
     if (p.phase_mode == PHASE_ROTATE) {
-        gsincos(p.c3y * V, &e.y, &e.x);
+        rotation(p, V, &e.y, &e.x);
     } else if (p.phase_mode == PHASE_DECAY) {
         e.x = gexp(p.c3x * V);
         e.y = (R)0;
     } else {
         R s, c;
         const R t = gexp(p.c3x * V);
-        gsincos(p.c3y * V, &s, &c);
+        rotation(p, V, &s, &c);
         e.x = t * c;
         e.y = t * s;
     }
