@@ -142,6 +142,14 @@ struct PassArgs {
     Phys<R> ph;
 };
 
+// The time-sliced additive potential at point idx, step `it` (F_VEXTRA), else 0.
+template <typename R> __device__ __forceinline__ R vextra_at(const PassArgs<R>& a, uint32_t idx, unsigned it) {
+    int s = (int)(it / (unsigned)a.vsteps);
+    if (s >= a.vslices) s = a.vslices - 1;
+    if (a.vring) s &= 1;
+    return a.vextra[((size_t)s << (a.lx + a.ly + a.lz)) | idx];
+}
+
 // External potential at step `it`: the built-in harmonic trap (per-axis tables), or the user hook
 // gpe_external_potential in a hook build; plus the time-sliced additive table when set.
 template <typename R> __device__ __forceinline__ R vext_at(const PassArgs<R>& a, uint32_t idx, int ix, int iy, int iz,
@@ -151,14 +159,43 @@ template <typename R> __device__ __forceinline__ R vext_at(const PassArgs<R>& a,
 #else
     R v = (__ldg(a.vx + ix) + __ldg(a.vy + iy)) + __ldg(a.vz + iz);
 #endif
-    if (a.flags & F_VEXTRA) {
-        int s = (int)(it / (unsigned)a.vsteps);
-        if (s >= a.vslices) s = a.vslices - 1;
-        if (a.vring) s &= 1;
-        v += a.vextra[((size_t)s << (a.lx + a.ly + a.lz)) | idx];
-    }
+    if (a.flags & F_VEXTRA) v += vextra_at(a, idx, it);
     return v;
 }
+
+// The same potential along one pencil (AX_X, AX_Y, AX_Z) or one plane row (AX = 3: ix and iy fixed):
+// the two trap terms that are constant there are read once per thread, so a point reads one table
+// entry; the sum keeps the order (vx + vy) + vz, so the values are those of vext_at.  FP32 only
+// (measured at 128^3: 93.1 -> 91.9 us per step; the FP64 corrector pass ran 4 % slower with it).
+template <typename R, int AX> struct PencilTrap {
+    static constexpr bool ROWS = (sizeof(R) == 4);
+    R c0 = (R)0, c1 = (R)0;
+    // (ix, iy, iz): a point of the pencil (any point: only its constant coordinates are used); called
+    // only for pencils inside the lattice
+    __device__ __forceinline__ void init(const PassArgs<R>& a, int ix, int iy, int iz) {
+#ifndef GPE_USER_HOOKS
+        if constexpr (!ROWS) { (void)a; (void)ix; (void)iy; (void)iz; }
+        else if constexpr (AX == 0) { c0 = __ldg(a.vy + iy); c1 = __ldg(a.vz + iz); }
+        else if constexpr (AX == 1) { c0 = __ldg(a.vx + ix); c1 = __ldg(a.vz + iz); }
+        else { c0 = __ldg(a.vx + ix) + __ldg(a.vy + iy); }
+#else
+        (void)a; (void)ix; (void)iy; (void)iz;
+#endif
+    }
+    __device__ __forceinline__ R at(const PassArgs<R>& a, uint32_t idx, int ix, int iy, int iz, unsigned it) const {
+#ifdef GPE_USER_HOOKS
+        return vext_at(a, idx, ix, iy, iz, it);
+#else
+        if constexpr (!ROWS) return vext_at(a, idx, ix, iy, iz, it);
+        R v;
+        if constexpr (AX == 0) v = (__ldg(a.vx + ix) + c0) + c1;
+        else if constexpr (AX == 1) v = (c0 + __ldg(a.vy + iy)) + c1;
+        else v = c0 + __ldg(a.vz + iz);
+        if (a.flags & F_VEXTRA) v += vextra_at(a, idx, it);
+        return v;
+#endif
+    }
+};
 
 // Mean field dE/drho at step `it`: built-in functional, or the user hook gpe_dEDFdn.
 template <typename R> __device__ __forceinline__ R mean_field(const PassArgs<R>& a, R rho, unsigned it) {
@@ -510,6 +547,12 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
     const unsigned it = dyn->it;
     const R s_prev = (R)dyn->s_prev;
     const bool scale_in = (a.flags & F_SCALE_IN) != 0;
+    PencilTrap<R, AX> trap;  // the trap terms constant along this pencil
+    if (valid) {
+        int ix0, iy0, iz0;
+        decode(at(0), ix0, iy0, iz0);
+        trap.init(a, ix0, iy0, iz0);
+    }
 
     C2<R> x[E];
 #pragma unroll
@@ -647,7 +690,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                 if (K == C_EPI && a.pre == PRE_VSTEP1) {
                     v = modify_at<R>(ix, iy, iz, it, v);
                     const R rho = density(a.ph, v);
-                    const R V = vext_at(a, idx, ix, iy, iz, it) + mean_field(a, rho, it);
+                    const R V = trap.at(a, idx, ix, iy, iz, it) + mean_field(a, rho, it);
                     a.V[idx] = V;
                     const C2<R> ph = phase(a.ph, V);
                     if (a.flags & F_PH_STORE) reinterpret_cast<C2<R>*>(a.aux)[idx] = ph;
@@ -656,7 +699,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                     C2<R> p2 = a.psi2[idx];
                     if (a.flags & F_SCALE_PSI2) p2 = cscale(p2, s2);
                     const R rho = density(a.ph, p2);
-                    R lv = (a.V[idx] + vext_at(a, idx, ix, iy, iz, it + 1)) + mean_field(a, rho, it + 1);
+                    R lv = (a.V[idx] + trap.at(a, idx, ix, iy, iz, it + 1)) + mean_field(a, rho, it + 1);
                     if (a.flags & F_QF) lv += a.Vqf[idx];
                     lv = (R)0.5 * lv;
                     const C2<R> e = phase(a.ph, lv);
@@ -811,7 +854,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
 #else
                     const R rho_m = rho;
 #endif
-                    const R V = (vext_at(a, idx, ix, iy, iz, it) + mean_field(a, rho_m, it)) + vqf;
+                    const R V = (trap.at(a, idx, ix, iy, iz, it) + mean_field(a, rho_m, it)) + vqf;
                     a.V[idx] = V;
                     const C2<R> ph = phase(a.ph, V);
                     if (a.flags & F_PH_STORE) reinterpret_cast<C2<R>*>(a.aux)[idx] = ph;
@@ -872,7 +915,7 @@ __device__ __forceinline__ void pass_body(const PassArgs<R>& a, uint32_t blk, ui
                     decode(idx, ix, iy, iz);
                     const C2<R> pp = cmul(own(q), phl ? ph : phase(a.ph, lv));
                     const R rho = density(a.ph, pp);
-                    lv = (lv + vext_at(a, idx, ix, iy, iz, it + 1)) + mean_field(a, rho, it + 1);
+                    lv = (lv + trap.at(a, idx, ix, iy, iz, it + 1)) + mean_field(a, rho, it + 1);
                     if (qfop) lv += vq;
                     lv = (R)0.5 * lv;
                     const C2<R> e = phase(a.ph, lv);

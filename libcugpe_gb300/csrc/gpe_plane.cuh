@@ -107,6 +107,8 @@ __global__ void __launch_bounds__(PlaneGeom<N>::NT, 1) plane_kernel(const PlaneA
 
     const DynState* dyn = a.dyn;
     const unsigned it = dyn->it;
+    PencilTrap<R, 3> trap;  // vx[ix] + vy[row], constant along the thread's row
+    trap.init(a, (int)ix, row, 0);
     C2<R> x[E];
 #pragma unroll
     for (int q = 0; q < E; q++) x[q] = a.in[at(q)];
@@ -133,7 +135,7 @@ __global__ void __launch_bounds__(PlaneGeom<N>::NT, 1) plane_kernel(const PlaneA
             const int iz = tr + T * q;
             C2<R> v = modify_at<R>((int)ix, row, iz, it, rcell(q));
             const R rho = density(a.ph, v);
-            const R V = vext_at(a, idx, (int)ix, row, iz, it) + mean_field(a, rho, it);
+            const R V = trap.at(a, idx, (int)ix, row, iz, it) + mean_field(a, rho, it);
             a.V[idx] = V;
             const C2<R> ph = phase(a.ph, V);
             if (a.flags & F_PH_STORE) reinterpret_cast<C2<R>*>(a.aux)[idx] = ph;
@@ -222,7 +224,7 @@ __global__ void __launch_bounds__(PlaneGeom<N>::NT, 1) plane_kernel(const PlaneA
                 }
                 const C2<R> pp = cmul(rcell(q), phl ? ph : phase(a.ph, lv));
                 const R rho = density(a.ph, pp);
-                lv = (lv + vext_at(a, idx, (int)ix, row, iz, it + 1)) + mean_field(a, rho, it + 1);
+                lv = (lv + trap.at(a, idx, (int)ix, row, iz, it + 1)) + mean_field(a, rho, it + 1);
                 if (qfop) lv += vq;
                 lv = (R)0.5 * lv;
                 const C2<R> e = phase(a.ph, lv);
