@@ -38,7 +38,7 @@ B_ALG = {  # algorithmic bytes per grid point per step (8 S + S + 4 s_r, + 4 S w
 }
 # warp instructions of one GPE step of the 128^3 FP32 friction step in the yz-plane layout (ncu
 # smsp__inst_executed.sum over its four launches, profiles/plane_and_pass_kernel_issue_bound_128_fp32_ufg_qf.md)
-INST_PER_STEP_128_PLANE = 59.3e6
+INST_PER_STEP_128_PLANE = 58.4e6
 
 
 def peaks():
